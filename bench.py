@@ -1,0 +1,387 @@
+#!/usr/bin/env python
+"""Headline benchmark: mixed-precision all-pairs gravity on one GB300.
+
+Workload (the mixed-precision direct configuration): N = 65,536 equal-mass
+Plummer sphere (G = 1, M = 1, a = 1, virial velocities, generator seed 0),
+softening 1e-3, velocity Verlet with dt = 5e-4.  One step = one velocity-Verlet
+step of the engine (the force of the new positions plus the two half-updates;
+the start-of-step force is the previous step's end force).  Interactions per
+step = N (N - 1).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is device-timed: CUDA events around
+each step on the simulation's stream, inputs resident in HBM, L2 flushed
+(a 256 MiB write) before every timed step.  `e2e` is one force evaluation
+through the public C ABI with pinned host buffers per step: nb_load (H2D of the
+7 input arrays) + nb_compute_forces + nb_read_state of the 3 acceleration
+arrays (D2H), wall clock.  `--impl reference` times the reference's CPU
+direct sum (its C restatement, the only CPU build of it that exists on the
+GPU host) on all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(REPO, "n-body-gravity-simulation_gb300")
+sys.path.insert(0, PKG_DIR)
+
+METRIC = "Ginteractions/s direct + BH N=2^20 steps/s, mixed vs FP64 GPU at stated err"
+UNIT = "Ginteractions/s"
+N_BODIES = 65536
+EPS = 1e-3
+DT = 5e-4
+SEED = 0
+WORKLOAD = "plummer_n65536_mixed_direct_velocity_verlet"
+FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=N_BODIES)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="target CPU time of the cpu_baseline sample")
+    ap.add_argument("--skip-extras", action="store_true",
+                    help="only the headline value (no FP64 / accuracy / energy extras)")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ["index", "clocks.sm", "clocks.max.sm", "power.draw",
+              "clocks_event_reasons.active", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device_index: int):
+        self.samples = []
+        self.proc = None
+        self.dev = device_index
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "100", "-i", str(self.dev)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == len(self.FIELDS):
+                self.samples.append((time.time(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self, t0: float, t1: float):
+        inside = [p for t, p in self.samples if t0 <= t <= t1]
+        if not inside and self.samples:  # short region: nearest samples
+            inside = [min(self.samples, key=lambda s: abs(s[0] - 0.5 * (t0 + t1)))[1]]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"],
+                    "samples": 0}
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        sm = [num(p[1]) for p in inside if num(p[1]) is not None]
+        smax = [num(p[2]) for p in inside if num(p[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for p in inside for k in range(4)
+                          if p[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(inside),
+                "power_w_max": max((num(p[3]) or 0.0) for p in inside)}
+
+
+# ---------------------------------------------------------------- helpers
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p)), "measured"
+        except ValueError:
+            pass
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def fp32_roofline_gint(num_sms: int, mhz: float) -> float:
+    """All-pairs roofline: 12 FP32-pipe operations per interaction (3 FADD for
+    the displacement, 3 FFMA for r^2, 3 FMUL for m r^-3, 3 FFMA to accumulate)
+    on 128 FP32 lanes per SM per clock; the one MUFU rsqrt per interaction
+    (16/clk/SM) does not bind."""
+    return num_sms * mhz * 1e6 * 128.0 / 12.0 / 1e9
+
+
+def cpu_reference_rate(n, target_seconds, threads=0):
+    """The reference's FP64 direct sum on the host cores (its C restatement),
+    timed on a bounded sample of i-rows of the same workload."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import nbody_gb300 as nb
+    import oracle as O
+    if not os.path.exists(O.LIB_PATH):
+        O.build(with_ref=False)
+    x, y, z, vx, vy, vz, m = nb.plummer(n, seed=SEED)
+    cores = O.threads() if threads == 0 else threads
+    rows = 256
+    t0 = time.perf_counter()
+    O.forces_naive_rows(x, y, z, m, 1.0, EPS, 0, rows, threads)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    rows = int(min(n, max(256, rows * target_seconds / dt)))
+    return x, y, z, m, rows, cores, O
+
+
+# ---------------------------------------------------------------- reference arm
+def run_reference(a, rank, world):
+    if rank != 0:
+        return 0
+    n = a.n
+    per_step = max(0.5, min(3.0, 60.0 / max(1, a.steps + a.warmup)))
+    x, y, z, m, rows, cores, O = cpu_reference_rate(n, per_step)
+    for _ in range(a.warmup):
+        O.forces_naive_rows(x, y, z, m, 1.0, EPS, 0, rows)
+    t0 = time.perf_counter()
+    for k in range(a.steps):
+        i0 = (k * rows) % max(1, n - rows + 1)
+        O.forces_naive_rows(x, y, z, m, 1.0, EPS, i0, i0 + rows)
+    elapsed = time.perf_counter() - t0
+    inter = a.steps * rows * (n - 1)
+    value = inter / elapsed / 1e9
+    sample = (f"{rows} of {n} i-rows x all {n} j per step (FP64 direct sum, the hot loop of the "
+              f"reference's CPU velocity-Verlet step), {a.steps} steps")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": elapsed / a.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "softening": EPS, "dt": DT,
+                   "integrator": "velocity_verlet", "method": "direct_fp64_cpu"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(a, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import nbody_gb300 as nb
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream(dev)
+    n = a.n
+    inter = n * (n - 1)
+    state = nb.plummer(n, seed=SEED)
+    cfg = nb.Config(method=nb.DIRECT_MIXED, G=1.0, softening=EPS)
+    sim = nb.Sim(cfg, capacity=n, stream=stream.cuda_stream)
+    sim.load(*state)
+    e_start = None if a.skip_extras else sim.diagnostics()
+
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(a.warmup):
+        sim.step(nb.VELOCITY_VERLET, DT, 1)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(0.3)
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sim.profile(True)
+    sim.profile_read(reset=True)
+    launches0 = nb.kernel_launch_count()
+    t_wall0 = time.time()
+    for k in range(a.steps):
+        flush.zero_()
+        ev0[k].record(stream)
+        sim.step(nb.VELOCITY_VERLET, DT, 1)
+        ev1[k].record(stream)
+    torch.cuda.synchronize()
+    t_wall1 = time.time()
+    launches = nb.kernel_launch_count() - launches0
+    prof = sim.profile_read(reset=True)
+    sim.profile(False)
+    clocks.stop()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in zip(ev0, ev1)]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * a.steps * inter / (total_ms / 1e3) / 1e9
+
+    # roofline of the dominant kernel (the all-pairs kernel)
+    props = torch.cuda.get_device_properties(local_rank)
+    peaks, peak_kind = measured_peaks()
+    kernel_ms = prof["force_kernel_ms"] / max(1, prof["force_launches"])
+    achieved = inter / (kernel_ms / 1e3) / 1e9
+    clk = clocks.summary(t_wall0, t_wall1)
+    peak = fp32_roofline_gint(props.multi_processor_count, peaks.get("sm_max_mhz", 2070.0))
+    roofline = {
+        "bound": "fp32", "kernel": "direct_mixed_kernel", "achieved": achieved,
+        "peak": peak, "unit": "Ginteractions/s", "frac": achieved / peak,
+        "peak_basis": (f"{props.multi_processor_count} SMs x {peaks.get('sm_max_mhz', 2070.0)}"
+                       f" MHz ({peak_kind} sm_max_mhz) x 128 FP32 lanes / 12 FP32 ops per "
+                       "interaction"),
+        "traffic": None,
+        "kernel_ms": kernel_ms,
+    }
+    if clk.get("sm_mhz"):
+        roofline["frac_at_measured_clock"] = achieved / fp32_roofline_gint(
+            props.multi_processor_count, clk["sm_mhz"])
+    tp = os.path.join(REPO, "profiles", "direct_mixed_n65536_traffic.json")
+    if os.path.exists(tp) and n == N_BODIES:
+        try:
+            roofline["traffic"] = json.load(open(tp)).get("dram_bytes_per_launch")
+        except ValueError:
+            pass
+
+    extras = {}
+    if not a.skip_extras and rank == 0:
+        e_end = sim.diagnostics()
+        extras["energy_drift"] = {
+            "steps": a.warmup + a.steps,
+            "rel": (e_end["total_softened"] - e_start["total_softened"]) /
+                   abs(e_start["total_softened"]),
+            "note": "softened total energy, FP64 GPU reduction, mixed-precision run"}
+        # accuracy and speed of the mixed kernel vs the FP64 kernel on the
+        # current state (the FP64 path is pinned to the CPU oracle at 1e-12 by
+        # the tests)
+        st = sim.read_state()
+        sim.compute_forces()
+        mixed_acc = sim.accelerations()
+        ref = nb.Sim(nb.Config(method=nb.DIRECT_FP64, G=1.0, softening=EPS), capacity=n,
+                     stream=stream.cuda_stream)
+        ref.load(st["x"], st["y"], st["z"], st["vx"], st["vy"], st["vz"], st["m"])
+        ref.compute_forces()  # warm
+        ref.profile(True)
+        ref.profile_read(reset=True)
+        ref.compute_forces()
+        p64 = ref.profile_read(reset=True)
+        ref_acc = ref.accelerations()
+        ref.close()
+        d = np.sqrt(sum((u - v) ** 2 for u, v in zip(mixed_acc, ref_acc)))
+        r = np.sqrt(sum(v * v for v in ref_acc))
+        rel = d / np.maximum(r, 1e-300)
+        fp64_rate = inter / (p64["force_kernel_ms"] / 1e3) / 1e9
+        extras["force_error_vs_fp64"] = {"max_rel": float(rel.max()),
+                                         "rms_rel": float(np.sqrt(np.mean(rel * rel))),
+                                         "max_abs_over_rms_a": float(d.max() /
+                                                                     np.sqrt(np.mean(r * r)))}
+        extras["fp64_direct"] = {"gint_s": fp64_rate, "kernel": "direct_fp64_kernel",
+                                 "mixed_speedup": achieved / fp64_rate}
+
+    # e2e: one force evaluation through the C ABI with pinned host buffers
+    e2e = None
+    if rank == 0:
+        host = [torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for v in state]
+        outs = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(3)]
+        ptr_in = [h.data_ptr() for h in host]
+        ptr_out = [0] * 6 + [o.data_ptr() for o in outs] + [0]
+        for _ in range(max(1, a.warmup)):
+            sim.load_pointers(n, ptr_in)
+            sim.compute_forces()
+            sim.read_pointers(ptr_out)
+        ke = min(a.steps, 200)
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            sim.load_pointers(n, ptr_in)
+            sim.compute_forces()
+            sim.read_pointers(ptr_out)
+        el = time.perf_counter() - t0
+        e2e = {"value": ke * inter / el / 1e9, "unit": UNIT, "h2d_bytes_per_step": 7 * 8 * n,
+               "d2h_bytes_per_step": 3 * 8 * n,
+               "step": "nb_load (7 FP64 arrays) + nb_compute_forces + nb_read_state "
+                       "(3 acceleration arrays), pinned host memory, wall clock"}
+
+    cpu = None
+    if rank == 0 and not a.skip_extras:
+        x, y, z, m, rows, cores, O = cpu_reference_rate(n, a.cpu_seconds)
+        t0 = time.perf_counter()
+        O.forces_naive_rows(x, y, z, m, 1.0, EPS, 0, rows)
+        el = time.perf_counter() - t0
+        cpu = {"value": rows * (n - 1) / el / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"FP64 direct sum of the reference (C restatement), {rows} of {n} "
+                         f"i-rows x all {n} j, one pass"}
+    sim.close()
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": total_ms / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+ds/f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "softening": EPS, "dt": DT, "G": 1.0,
+                   "integrator": "velocity_verlet", "method": "direct_mixed",
+                   "parallelism": "replicas" if world > 1 else "single_gpu",
+                   "l2": "flushed (256 MiB write) before every timed step",
+                   "timing": "CUDA events per step on the simulation stream"},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    line.update(extras)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    a = parse()
+    rank, world, local_rank = dist_env()
+    if a.impl == "reference":
+        return run_reference(a, rank, world)
+    return run_ours(a, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,245 @@
+/*
+ * nbody_c.h -- C ABI of the GB300 N-body engine.
+ *
+ * This is the drop-in boundary for the force-and-step hot path of
+ * PawanKiitb/N-body-gravity-simulation.  The reference has no C ABI; its
+ * boundary is the C++ host API in CUDA/include/.  Each entry point below names
+ * the reference interface it replaces.  The C++ classes of that API
+ * (ParticleArrays, ForceCalculatorNaive, BarnesHutForceCalculator, the
+ * integrators) are re-implemented on top of this ABI by the package's compat
+ * layer.
+ *
+ * Conventions
+ *   - Every function returns nb_status; nb_last_error() gives the message of
+ *     the most recent failure on the calling thread.
+ *   - Arrays are structure-of-arrays FP64, one value per body, as in the
+ *     reference (ParticleArrays, CUDA/include/particle_data.hpp:6-43).
+ *   - Work is enqueued on the simulation's CUDA stream (the `stream`
+ *     argument of nb_create; NULL = the legacy default stream, which is what
+ *     the reference uses).  Functions that return host data synchronise that
+ *     stream; the others are asynchronous.  nb_synchronize() waits.
+ *   - A simulation object is not thread-safe; distinct objects are.
+ *   - No function prints or exits; a device-side failure (tree or stack
+ *     capacity) is reported as NB_ERR_DEVICE_FAULT at the next synchronising
+ *     call.
+ */
+#ifndef NBODY_C_H
+#define NBODY_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum nb_status {
+    NB_OK = 0,
+    NB_ERR_INVALID_ARGUMENT = 1,
+    NB_ERR_CUDA = 2,
+    NB_ERR_OUT_OF_MEMORY = 3,
+    NB_ERR_CAPACITY = 4,     /* more bodies than the object was created for */
+    NB_ERR_NOT_LOADED = 5,   /* no bodies loaded yet */
+    NB_ERR_DEVICE_FAULT = 6, /* a kernel reported an error status */
+    NB_ERR_UNSUPPORTED = 7
+} nb_status;
+
+/* Force methods.
+ *   NB_DIRECT_FP64  : all-pairs sum in FP64 (the 1e-12 path; the reference's
+ *                     computeAccelerationNaiveKernel, force_calculator_naive.cu:4-59).
+ *   NB_DIRECT_MIXED : all-pairs sum with FP32 pair arithmetic on double-single
+ *                     displacements, Kahan-compensated FP32 accumulation across
+ *                     j-tiles, FP64 combine (the 1e-6 path).
+ *   NB_BARNES_HUT   : 63-bit Morton octree, monopole, FP32 walk, FP64 result
+ *                     (replaces BarnesHutForceCalculator, force_calculator_barnes_hut.cu). */
+typedef enum nb_method {
+    NB_DIRECT_FP64 = 0,
+    NB_DIRECT_MIXED = 1,
+    NB_BARNES_HUT = 2
+} nb_method;
+
+/* Integrators, the reference's TimeIntegrator family
+ * (CUDA/include/integrator.hpp:7-17, CPU/src/integrator_rk4.cpp). */
+typedef enum nb_integrator {
+    NB_EULER = 0,
+    NB_EULER_CROMER = 1,
+    NB_LEAPFROG = 2,         /* kick-drift-kick */
+    NB_VELOCITY_VERLET = 3,
+    NB_RK4 = 4
+} nb_integrator;
+
+typedef struct nb_config {
+    int method;         /* nb_method */
+    double G;           /* gravitational constant; the reference uses 4 pi^2 */
+    double softening;   /* epsilon (the pair term uses epsilon^2), ForceCalculator(double softening) */
+    double theta;       /* Barnes-Hut opening angle, BarnesHutForceCalculator(.., theta, ..) */
+    int leaf_capacity;  /* Barnes-Hut bodies per leaf (reference default 8) */
+    int flags;          /* NB_FLAG_* */
+} nb_config;
+
+/* flags */
+#define NB_FLAG_NONE 0
+/* Report the reference's unsoftened potential energy as `potential` (default:
+ * both are always reported, see nb_diag). */
+#define NB_FLAG_RESERVED 1
+
+typedef struct nb_sim nb_sim;
+
+/* Energies and moments of the current state, reduced on the GPU in FP64.
+ * Replaces the host loops of CUDA/src/test_common.cpp:63-182. */
+typedef struct nb_diag {
+    double kinetic;            /* sum 1/2 m v^2 */
+    double potential;          /* -G sum_{i<j} m_i m_j / r_ij (unsoftened, as the reference) */
+    double potential_softened; /* -G sum_{i<j} m_i m_j / sqrt(r_ij^2 + eps^2): conserved when eps > 0 */
+    double total;              /* kinetic + potential */
+    double total_softened;     /* kinetic + potential_softened */
+    double angular_momentum[3];
+    double center_of_mass[3];
+    double momentum[3];
+    double mass;
+} nb_diag;
+
+/* ---- configuration and lifetime ---------------------------------------- */
+
+/* G = 1, softening 0, theta 0.5, leaf capacity 8, method NB_DIRECT_MIXED. */
+nb_status nb_config_default(nb_config *cfg);
+
+/* Creates a simulation able to hold up to `capacity` bodies on the current
+ * CUDA device.  Replaces allocateParticles (CUDA/src/particle_data.cu:6-43)
+ * together with the calculator constructors. */
+nb_status nb_create(const nb_config *cfg, size_t capacity, void *stream, nb_sim **out);
+
+/* Replaces freeParticles (CUDA/src/particle_data.cu:46-92) and the calculator
+ * destructors. */
+nb_status nb_destroy(nb_sim *sim);
+
+/* Changes method / G / softening / theta / leaf capacity between steps. */
+nb_status nb_set_config(nb_sim *sim, const nb_config *cfg);
+nb_status nb_get_config(const nb_sim *sim, nb_config *cfg);
+
+/* ---- particle load and readback ---------------------------------------- */
+
+/* Copies n bodies from host FP64 arrays; zeroes accelerations.  Replaces
+ * copyParticlesToDevice (CUDA/src/particle_data.cu:95-119). */
+nb_status nb_load(nb_sim *sim, size_t n, const double *x, const double *y, const double *z,
+                  const double *vx, const double *vy, const double *vz, const double *m);
+
+/* Same from device pointers (device-to-device copies). */
+nb_status nb_load_device(nb_sim *sim, size_t n, const double *x, const double *y,
+                         const double *z, const double *vx, const double *vy, const double *vz,
+                         const double *m);
+
+/* Copies the state to host arrays; any pointer may be NULL to skip that
+ * field.  Replaces copyParticlesToHost (CUDA/src/particle_data.cu:122-143). */
+nb_status nb_read_state(nb_sim *sim, double *x, double *y, double *z, double *vx, double *vy,
+                        double *vz, double *ax, double *ay, double *az, double *m);
+
+/* Device pointers of the FP64 state arrays (valid until nb_destroy):
+ * order x y z vx vy vz ax ay az m. */
+nb_status nb_device_arrays(nb_sim *sim, double **ptrs10);
+
+nb_status nb_num_bodies(const nb_sim *sim, size_t *n);
+
+/* ---- hot path ----------------------------------------------------------- */
+
+/* Accelerations of the current positions into the acceleration arrays.
+ * Replaces ForceCalculator::computeAccelerations
+ * (CUDA/include/force_calculator.hpp:24-26; force_calculator_naive.cu:61-92;
+ * force_calculator_barnes_hut.cu:625-671). */
+nb_status nb_compute_forces(nb_sim *sim);
+
+/* nsteps steps of the integrator with time step dt.  Replaces
+ * TimeIntegrator::step (CUDA/include/integrator.hpp:9-13).  Leapfrog and
+ * velocity Verlet reuse the acceleration of the previous step when it is
+ * still valid (as integrator_leafrog.cu:59-62 does with is_first_step);
+ * Euler, Euler-Cromer and RK4 evaluate it at the start of every step. */
+nb_status nb_step(nb_sim *sim, int integrator, double dt, int nsteps);
+
+/* Marks the stored accelerations stale (after the caller edited positions
+ * through nb_device_arrays). */
+nb_status nb_invalidate_forces(nb_sim *sim);
+
+nb_status nb_synchronize(nb_sim *sim);
+
+/* ---- diagnostics --------------------------------------------------------- */
+
+/* Replaces kineticEnergy / potentialEnergy / totalEnergy / angularMomentum /
+ * centerOfMass (CUDA/src/test_common.cpp:63-182). */
+nb_status nb_diagnostics(nb_sim *sim, nb_diag *out);
+
+/* ---- Barnes-Hut introspection (tests and tools) -------------------------- */
+
+typedef struct nb_bh_info {
+    int num_nodes;
+    int num_leaves;
+    int max_depth;
+    int split_levels;   /* levels the root cube may split (<= 21) */
+    double root[4];     /* centre x, y, z and side of the root cube */
+} nb_bh_info;
+
+/* Builds the tree of the current positions (without a walk) and reports it. */
+nb_status nb_bh_build(nb_sim *sim, nb_bh_info *info);
+
+/* After nb_bh_build or a Barnes-Hut force evaluation: the sorted 63-bit
+ * Morton codes and the original index of each sorted body (host arrays of
+ * n entries; either may be NULL). */
+nb_status nb_bh_read_order(nb_sim *sim, uint64_t *sorted_codes, uint32_t *order);
+
+/* Node table in breadth-first order (host arrays of max_nodes entries; any
+ * may be NULL): depth, Morton prefix, first sorted body, body count, leaf
+ * flag, first child, child count; com_mass gets 4 floats per node (COM xyz,
+ * mass).  Returns NB_ERR_CAPACITY when max_nodes is too small. */
+nb_status nb_bh_read_nodes(nb_sim *sim, int max_nodes, int *depth, uint64_t *prefix,
+                           int *first, int *count, int *is_leaf, int *first_child,
+                           int *nchild, float *com_mass);
+
+/* ---- host-side input generators (no GPU needed) ------------------------- */
+
+/* Equal-mass Plummer sphere (total mass M, scale radius a, G), positions and
+ * velocities by the Aarseth-Henon-Wielen (1974) construction, centred on the
+ * centre of mass.  Random numbers: SplitMix64 keyed by (seed, body, draw). */
+nb_status nb_gen_plummer(size_t n, uint64_t seed, double total_mass, double scale, double G,
+                         double *x, double *y, double *z, double *vx, double *vy, double *vz,
+                         double *m);
+
+/* Bulge (Plummer, mass fraction bulge_frac, scale bulge_scale) plus an
+ * exponential disk (scale length disk_scale, sech^2 height disk_height) with
+ * circular velocities from the enclosed mass plus isotropic dispersion
+ * `dispersion` (in units of the local circular speed). */
+nb_status nb_gen_disk_bulge(size_t n, uint64_t seed, double total_mass, double bulge_frac,
+                            double bulge_scale, double disk_scale, double disk_height,
+                            double dispersion, double G, double *x, double *y, double *z,
+                            double *vx, double *vy, double *vz, double *m);
+
+/* ---- measurement ---------------------------------------------------------- */
+
+/* Device time of the dominant force kernel (the all-pairs kernel or the tree
+ * walk) of every evaluation while profiling is enabled, from CUDA events
+ * recorded on the simulation's stream around that launch.  The reference
+ * keeps the same totals in its calculators (getTotalComputeTime,
+ * force_calculator_naive.hpp:23-25), but synchronises after every call. */
+typedef struct nb_profile {
+    uint64_t kernel_launches;  /* this library's kernel launches in the process so far */
+    uint64_t force_launches;   /* timed force-kernel launches since the last reset */
+    double force_kernel_ms;    /* their summed device time */
+} nb_profile;
+
+nb_status nb_profile_enable(nb_sim *sim, int enable);
+/* Synchronises the stream; reset != 0 starts a new window. */
+nb_status nb_profile_read(nb_sim *sim, nb_profile *out, int reset);
+/* Process-wide count of kernel launches made by this library. */
+uint64_t nb_kernel_launch_count(void);
+
+/* ---- errors --------------------------------------------------------------- */
+
+const char *nb_status_string(nb_status s);
+const char *nb_last_error(void);
+
+/* Library version string. */
+const char *nb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBODY_C_H */

@@ -1,0 +1,380 @@
+// nb_direct.cu -- all-pairs gravity on sm_103a.
+//
+// Replaces computeAccelerationNaiveKernel (CUDA/src/force_calculator_naive.cu:4-59,
+// one FP64 thread per body, 256-body tiles, ceil(N/256) CTAs).  Two kernels:
+//
+//  * direct_mixed_kernel -- the production path.  Each body is held as a float4
+//    "hi" (x, y, z, m) plus a float4 "lo" (x - hi, ...): a double-single copy of
+//    its FP64 position.  The pair displacement is formed as
+//    (xj_hi - xi_hi) + (xj_lo - xi_lo), which is exact to FP32 rounding for close
+//    pairs, so close encounters keep a relative force error near 1e-7 however far
+//    the pair is from the origin.  The rest of the pair term is plain FP32 on the
+//    FMA pipe with one MUFU rsqrt (rsqrt.approx.ftz.f32).  Every thread owns
+//    IPT i-bodies, so one broadcast shared-memory read of a j-body feeds IPT pair
+//    terms.  Per j-tile the FP32 tile sum is added into a Kahan-compensated
+//    (sum, compensation) pair; the CTA's partial over its j-segment is written
+//    as FP32 (sum, comp) and the segments are combined in FP64.
+//    The tensor cores stay idle: a softened 1/r^3 sum is not a contraction.
+//
+//  * direct_fp64_kernel -- the 1e-12 path: the same tiling in FP64.
+//
+// Grid: x = i-blocks of BLOCK*IPT bodies, y = j-segments.  The j-split keeps
+// all 152 SMs busy at small N (the reference runs 4 CTAs at N = 1024) and the
+// segment count is chosen to fill whole waves.
+#include "nb_internal.h"
+
+#include <algorithm>
+#include <cmath>
+
+namespace nb {
+namespace {
+
+__device__ __forceinline__ float rsqrt_mufu(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Padding body for the tail of the last tile: massless and far away, so that
+// its pair term is exactly zero (s = 0 * finite) for every i-body.
+__device__ __forceinline__ float4 far_body() { return make_float4(1.0e18f, 1.0e18f, 1.0e18f, 0.0f); }
+
+// Kahan-compensated add of t into (s, c).  Plain FP32 adds: no product, so
+// nothing can be contracted into an FMA.
+__device__ __forceinline__ void kahan_add(float &s, float &c, float t)
+{
+    float y = t - c;
+    float u = s + y;
+    c = (u - s) - y;
+    s = u;
+}
+
+template <int BLOCK, int IPT, bool ZERO_SOFT>
+__global__ void __launch_bounds__(BLOCK)
+direct_mixed_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo, int n,
+                    float eps2, int seg_len, float *__restrict__ psum,
+                    float *__restrict__ pcomp)
+{
+    __shared__ float4 sh_hi[BLOCK];
+    __shared__ float4 sh_lo[BLOCK];
+
+    const int tid = threadIdx.x;
+    const int ibase = blockIdx.x * (BLOCK * IPT);
+
+    float xh[IPT], yh[IPT], zh[IPT], xl[IPT], yl[IPT], zl[IPT];
+    float sx[IPT], sy[IPT], sz[IPT], cx[IPT], cy[IPT], cz[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = ibase + k * BLOCK + tid;
+        float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
+        if (i < n) {
+            h = hi[i];
+            l = lo[i];
+        }
+        xh[k] = h.x; yh[k] = h.y; zh[k] = h.z;
+        xl[k] = l.x; yl[k] = l.y; zl[k] = l.z;
+        sx[k] = sy[k] = sz[k] = 0.f;
+        cx[k] = cy[k] = cz[k] = 0.f;
+    }
+
+    const int j0 = blockIdx.y * seg_len;
+    const int j1 = min(n, j0 + seg_len);
+    for (int t0 = j0; t0 < j1; t0 += BLOCK) {
+        const int j = t0 + tid;
+        float4 h = far_body(), l = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (j < j1) {
+            h = hi[j];
+            l = lo[j];
+        }
+        __syncthreads();
+        sh_hi[tid] = h;
+        sh_lo[tid] = l;
+        __syncthreads();
+
+        float ax[IPT], ay[IPT], az[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) ax[k] = ay[k] = az[k] = 0.f;
+
+#pragma unroll 4
+        for (int jj = 0; jj < BLOCK; ++jj) {
+            const float4 H = sh_hi[jj];
+            const float4 L = sh_lo[jj];
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const float dx = (H.x - xh[k]) + (L.x - xl[k]);
+                const float dy = (H.y - yh[k]) + (L.y - yl[k]);
+                const float dz = (H.z - zh[k]) + (L.z - zl[k]);
+                const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+                float inv = rsqrt_mufu(r2);
+                if (ZERO_SOFT) inv = (r2 > 0.f) ? inv : 0.f;  // the j == i term
+                const float inv2 = inv * inv;
+                const float s = (H.w * inv) * inv2;
+                ax[k] = fmaf(dx, s, ax[k]);
+                ay[k] = fmaf(dy, s, ay[k]);
+                az[k] = fmaf(dz, s, az[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            kahan_add(sx[k], cx[k], ax[k]);
+            kahan_add(sy[k], cy[k], ay[k]);
+            kahan_add(sz[k], cz[k], az[k]);
+        }
+    }
+
+    const size_t plane = (size_t)n;
+    const size_t base = (size_t)blockIdx.y * 3 * plane;
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = ibase + k * BLOCK + tid;
+        if (i < n) {
+            psum[base + i] = sx[k];
+            psum[base + plane + i] = sy[k];
+            psum[base + 2 * plane + i] = sz[k];
+            pcomp[base + i] = cx[k];
+            pcomp[base + plane + i] = cy[k];
+            pcomp[base + 2 * plane + i] = cz[k];
+        }
+    }
+}
+
+// a_i = G * sum_s (sum_s - comp_s), in FP64, segments in index order.
+__global__ void combine_mixed_kernel(const float *__restrict__ psum,
+                                     const float *__restrict__ pcomp, int n, int segments,
+                                     double G, double *__restrict__ ax,
+                                     double *__restrict__ ay, double *__restrict__ az)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t plane = (size_t)n;
+    double a[3] = {0.0, 0.0, 0.0};
+    for (int s = 0; s < segments; ++s) {
+        const size_t base = (size_t)s * 3 * plane;
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            a[c] += (double)psum[base + c * plane + i] - (double)pcomp[base + c * plane + i];
+    }
+    ax[i] = G * a[0];
+    ay[i] = G * a[1];
+    az[i] = G * a[2];
+}
+
+template <int BLOCK, int IPT, bool ZERO_SOFT>
+__global__ void __launch_bounds__(BLOCK)
+direct_fp64_kernel(const double *__restrict__ x, const double *__restrict__ y,
+                   const double *__restrict__ z, const double *__restrict__ m, int n,
+                   double eps2, int seg_len, double *__restrict__ part)
+{
+    __shared__ double4 sh[BLOCK];
+    const int tid = threadIdx.x;
+    const int ibase = blockIdx.x * (BLOCK * IPT);
+    double xi[IPT], yi[IPT], zi[IPT], ax[IPT], ay[IPT], az[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = ibase + k * BLOCK + tid;
+        xi[k] = (i < n) ? x[i] : 0.0;
+        yi[k] = (i < n) ? y[i] : 0.0;
+        zi[k] = (i < n) ? z[i] : 0.0;
+        ax[k] = ay[k] = az[k] = 0.0;
+    }
+    const int j0 = blockIdx.y * seg_len;
+    const int j1 = min(n, j0 + seg_len);
+    for (int t0 = j0; t0 < j1; t0 += BLOCK) {
+        const int j = t0 + tid;
+        double4 b = make_double4(1.0e150, 1.0e150, 1.0e150, 0.0);
+        if (j < j1) b = make_double4(x[j], y[j], z[j], m[j]);
+        __syncthreads();
+        sh[tid] = b;
+        __syncthreads();
+#pragma unroll 2
+        for (int jj = 0; jj < BLOCK; ++jj) {
+            const double4 B = sh[jj];
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const double dx = B.x - xi[k];
+                const double dy = B.y - yi[k];
+                const double dz = B.z - zi[k];
+                const double r2 = fma(dz, dz, fma(dy, dy, fma(dx, dx, eps2)));
+                double inv = rsqrt(r2);
+                if (ZERO_SOFT) inv = (r2 > 0.0) ? inv : 0.0;
+                const double s = B.w * inv * inv * inv;
+                ax[k] = fma(dx, s, ax[k]);
+                ay[k] = fma(dy, s, ay[k]);
+                az[k] = fma(dz, s, az[k]);
+            }
+        }
+    }
+    const size_t plane = (size_t)n;
+    const size_t base = (size_t)blockIdx.y * 3 * plane;
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = ibase + k * BLOCK + tid;
+        if (i < n) {
+            part[base + i] = ax[k];
+            part[base + plane + i] = ay[k];
+            part[base + 2 * plane + i] = az[k];
+        }
+    }
+}
+
+__global__ void combine_fp64_kernel(const double *__restrict__ part, int n, int segments,
+                                    double G, double *__restrict__ ax, double *__restrict__ ay,
+                                    double *__restrict__ az)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t plane = (size_t)n;
+    double a[3] = {0.0, 0.0, 0.0};
+    for (int s = 0; s < segments; ++s) {
+        const size_t base = (size_t)s * 3 * plane;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) a[c] += part[base + c * plane + i];
+    }
+    ax[i] = G * a[0];
+    ay[i] = G * a[1];
+    az[i] = G * a[2];
+}
+
+__global__ void split_kernel(const double *__restrict__ x, const double *__restrict__ y,
+                             const double *__restrict__ z, const double *__restrict__ m, int n,
+                             float4 *__restrict__ hi, float4 *__restrict__ lo)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double X = x[i], Y = y[i], Z = z[i];
+    const float hx = __double2float_rn(X), hy = __double2float_rn(Y), hz = __double2float_rn(Z);
+    hi[i] = make_float4(hx, hy, hz, __double2float_rn(m[i]));
+    lo[i] = make_float4(__double2float_rn(X - (double)hx), __double2float_rn(Y - (double)hy),
+                        __double2float_rn(Z - (double)hz), 0.0f);
+}
+
+// Picks the j-split so that i-blocks x segments fills whole waves of
+// `slots` resident CTAs; longer segments are preferred on ties.
+int pick_segments(int iblocks, int tiles, int slots)
+{
+    int best = 1;
+    double best_eff = -1.0;
+    const int smax = std::max(1, std::min(tiles, 64));
+    for (int s = 1; s <= smax; ++s) {
+        const int seg_tiles = (tiles + s - 1) / s;
+        const int s_eff = (tiles + seg_tiles - 1) / seg_tiles;
+        const long ctas = (long)iblocks * s_eff;
+        const long waves = (ctas + slots - 1) / slots;
+        // useful work / (waves * slots * longest segment): tail and
+        // quantisation losses; a small penalty per extra segment.
+        const double eff = (double)tiles * iblocks / ((double)waves * slots * seg_tiles) -
+                           0.002 * s_eff;
+        if (eff > best_eff + 1e-9) {
+            best_eff = eff;
+            best = s_eff;
+        }
+    }
+    return best;
+}
+
+template <int BLOCK, int IPT>
+int resident_ctas(const void *fn)
+{
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BLOCK, 0);
+    return std::max(1, per_sm) * device_props().num_sms;
+}
+
+constexpr int kMixBlock = 256;
+constexpr int kMixIpt = 4;
+constexpr int kF64Block = 128;
+constexpr int kF64Ipt = 2;
+
+} // namespace
+
+DirectPlan direct_mixed_plan(int n)
+{
+    DirectPlan p;
+    p.block = kMixBlock;
+    p.ipt = kMixIpt;
+    const int per_cta = p.block * p.ipt;
+    const int iblocks = (n + per_cta - 1) / per_cta;
+    const int tiles = (n + p.block - 1) / p.block;
+    static int slots = 0;
+    if (!slots)
+        slots = resident_ctas<kMixBlock, kMixIpt>(
+            (const void *)direct_mixed_kernel<kMixBlock, kMixIpt, false>);
+    p.segments = pick_segments(iblocks, tiles, slots);
+    p.seg_tiles = (tiles + p.segments - 1) / p.segments;
+    p.segments = (tiles + p.seg_tiles - 1) / p.seg_tiles;
+    return p;
+}
+
+nb_status split_positions(const double *x, const double *y, const double *z, const double *m,
+                          int n, float4 *hi, float4 *lo, cudaStream_t st)
+{
+    if (n <= 0) return NB_OK;
+    split_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, m, n, hi, lo);
+    NB_LAUNCH_CHECK();
+    return NB_OK;
+}
+
+nb_status direct_mixed(const float4 *hi, const float4 *lo, int n, double G, double eps2,
+                       double *ax, double *ay, double *az, DevBuf &partials, cudaStream_t st,
+                       const KernelTimer *timer, const DirectPlan *plan_override)
+{
+    if (n <= 0) return NB_OK;
+    const DirectPlan p = plan_override ? *plan_override : direct_mixed_plan(n);
+    if (p.block != kMixBlock || p.ipt != kMixIpt)
+        return fail(NB_ERR_UNSUPPORTED, "direct_mixed: unsupported tile shape");
+    NB_TRY(partials.reserve(sizeof(float) * 6 * (size_t)n * p.segments));
+    float *psum = partials.as<float>();
+    float *pcomp = psum + 3 * (size_t)n * p.segments;
+    const int per_cta = p.block * p.ipt;
+    dim3 grid((n + per_cta - 1) / per_cta, p.segments);
+    const int seg_len = p.seg_tiles * p.block;
+    if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
+    if (eps2 > 0.0)
+        direct_mixed_kernel<kMixBlock, kMixIpt, false>
+            <<<grid, kMixBlock, 0, st>>>(hi, lo, n, (float)eps2, seg_len, psum, pcomp);
+    else
+        direct_mixed_kernel<kMixBlock, kMixIpt, true>
+            <<<grid, kMixBlock, 0, st>>>(hi, lo, n, 0.0f, seg_len, psum, pcomp);
+    NB_LAUNCH_CHECK();
+    if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
+    combine_mixed_kernel<<<(n + 255) / 256, 256, 0, st>>>(psum, pcomp, n, p.segments, G, ax, ay,
+                                                         az);
+    NB_LAUNCH_CHECK();
+    return NB_OK;
+}
+
+nb_status direct_fp64(const double *x, const double *y, const double *z, const double *m, int n,
+                      double G, double eps2, double *ax, double *ay, double *az,
+                      DevBuf &partials, cudaStream_t st, const KernelTimer *timer)
+{
+    if (n <= 0) return NB_OK;
+    const int per_cta = kF64Block * kF64Ipt;
+    const int iblocks = (n + per_cta - 1) / per_cta;
+    const int tiles = (n + kF64Block - 1) / kF64Block;
+    static int slots = 0;
+    if (!slots)
+        slots = resident_ctas<kF64Block, kF64Ipt>(
+            (const void *)direct_fp64_kernel<kF64Block, kF64Ipt, false>);
+    int segs = pick_segments(iblocks, tiles, slots);
+    const int seg_tiles = (tiles + segs - 1) / segs;
+    segs = (tiles + seg_tiles - 1) / seg_tiles;
+    NB_TRY(partials.reserve(sizeof(double) * 3 * (size_t)n * segs));
+    double *part = partials.as<double>();
+    dim3 grid(iblocks, segs);
+    const int seg_len = seg_tiles * kF64Block;
+    if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
+    if (eps2 > 0.0)
+        direct_fp64_kernel<kF64Block, kF64Ipt, false>
+            <<<grid, kF64Block, 0, st>>>(x, y, z, m, n, eps2, seg_len, part);
+    else
+        direct_fp64_kernel<kF64Block, kF64Ipt, true>
+            <<<grid, kF64Block, 0, st>>>(x, y, z, m, n, 0.0, seg_len, part);
+    NB_LAUNCH_CHECK();
+    if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
+    combine_fp64_kernel<<<(n + 255) / 256, 256, 0, st>>>(part, n, segs, G, ax, ay, az);
+    NB_LAUNCH_CHECK();
+    return NB_OK;
+}
+
+} // namespace nb

@@ -1,0 +1,181 @@
+// nb_internal.h -- internal declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/nbody_c.h"
+
+namespace nb {
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string &msg);
+nb_status fail(nb_status s, const std::string &msg);
+nb_status cuda_fail(cudaError_t e, const char *what);
+
+#define NB_CUDA_TRY(call)                                                  \
+    do {                                                                   \
+        cudaError_t nb_e_ = (call);                                        \
+        if (nb_e_ != cudaSuccess) return ::nb::cuda_fail(nb_e_, #call);    \
+    } while (0)
+
+// Counts one kernel launch of this library and checks the launch status.
+void count_launch();
+#define NB_LAUNCH_CHECK()                                                  \
+    do {                                                                   \
+        ::nb::count_launch();                                              \
+        cudaError_t nb_e_ = cudaGetLastError();                            \
+        if (nb_e_ != cudaSuccess) return ::nb::cuda_fail(nb_e_, "kernel launch"); \
+    } while (0)
+
+#define NB_TRY(call)                                                       \
+    do {                                                                   \
+        nb_status nb_s_ = (call);                                          \
+        if (nb_s_ != NB_OK) return nb_s_;                                  \
+    } while (0)
+
+// Device status word codes written by kernels (never trap, never hang).
+enum DeviceError : int {
+    kDevOk = 0,
+    kDevStackOverflow = 1,   // Barnes-Hut walk stack full
+    kDevTreeOverflow = 2,    // more nodes than the node buffer holds
+    kDevBadInput = 3,        // non-finite coordinates
+};
+
+// ---------------------------------------------------------------- memory
+// A device buffer that grows on demand and is freed with its owner.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    nb_status reserve(size_t want);
+    void release();
+    template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+struct DeviceProps {
+    int device = 0;
+    int num_sms = 0;
+    int max_smem_optin = 0;
+};
+const DeviceProps &device_props();
+
+// A pair of events recorded around the dominant kernel of a force evaluation
+// (null members: not recorded).
+struct KernelTimer {
+    cudaEvent_t start = nullptr, stop = nullptr;
+};
+
+// ---------------------------------------------------------------- direct sum
+struct DirectPlan {
+    int block = 256;    // threads per CTA
+    int ipt = 4;        // i-bodies per thread
+    int segments = 1;   // j-split factor (CTAs along y)
+    int seg_tiles = 1;  // j-tiles per segment
+};
+
+// Mixed FP32/double-single all-pairs kernel.  hi/lo: float4 (x, y, z, m) and
+// (x_lo, y_lo, z_lo, 0) of every body.  Writes G * sum into ax/ay/az (FP64).
+nb_status direct_mixed(const float4 *hi, const float4 *lo, int n, double G, double eps2,
+                       double *ax, double *ay, double *az, DevBuf &partials,
+                       cudaStream_t st, const KernelTimer *timer = nullptr,
+                       const DirectPlan *plan_override = nullptr);
+DirectPlan direct_mixed_plan(int n);
+
+// FP64 all-pairs kernel.
+nb_status direct_fp64(const double *x, const double *y, const double *z, const double *m,
+                      int n, double G, double eps2, double *ax, double *ay, double *az,
+                      DevBuf &partials, cudaStream_t st, const KernelTimer *timer = nullptr);
+
+// Builds the float4 hi/lo mirror of FP64 positions + masses.
+nb_status split_positions(const double *x, const double *y, const double *z,
+                          const double *m, int n, float4 *hi, float4 *lo, cudaStream_t st);
+
+// ---------------------------------------------------------------- integrators
+nb_status kick_drift(int kind, int n, double dt, double *x, double *y, double *z, double *vx,
+                     double *vy, double *vz, const double *ax, const double *ay,
+                     const double *az, double *oax, double *oay, double *oaz,
+                     cudaStream_t st);
+nb_status kick(int kind, int n, double dt, double *vx, double *vy, double *vz,
+               const double *ax, const double *ay, const double *az, const double *oax,
+               const double *oay, const double *oaz, cudaStream_t st);
+
+// RK4 stage kernels.  stage 2/3/4 positions/velocities from the base state.
+nb_status rk4_stage(int n, double h, const double *x, const double *y, const double *z,
+                    const double *vx, const double *vy, const double *vz, const double *kvx,
+                    const double *kvy, const double *kvz, const double *kax,
+                    const double *kay, const double *kaz, double *ox, double *oy,
+                    double *oz, double *ovx, double *ovy, double *ovz, cudaStream_t st);
+nb_status rk4_combine(int n, double dt, double *x, double *y, double *z, double *vx,
+                      double *vy, double *vz, const double *ax, const double *ay,
+                      const double *az, const double *k2, const double *k3, const double *k4,
+                      cudaStream_t st);
+
+// ---------------------------------------------------------------- diagnostics
+nb_status diagnostics(const double *x, const double *y, const double *z, const double *vx,
+                      const double *vy, const double *vz, const double *m, int n, double G,
+                      double eps2, DevBuf &scratch, cudaStream_t st, nb_diag *out);
+
+// ---------------------------------------------------------------- Barnes-Hut
+struct BHTree;  // opaque, defined in nb_bh.cu
+BHTree *bh_create();
+void bh_destroy(BHTree *t);
+// Builds the tree of (x,y,z,m) and, when ax != nullptr, walks it writing
+// G * acceleration (FP64) in the original body order.
+nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *z,
+                     const double *m, int n, double G, double eps2, double theta,
+                     int leaf_capacity, double *ax, double *ay, double *az, cudaStream_t st,
+                     const KernelTimer *timer = nullptr);
+nb_status bh_info(BHTree *t, cudaStream_t st, nb_bh_info *info);
+nb_status bh_read_order(BHTree *t, cudaStream_t st, uint64_t *codes, uint32_t *order);
+nb_status bh_read_nodes(BHTree *t, cudaStream_t st, int max_nodes, int *depth,
+                        uint64_t *prefix, int *first, int *count, int *is_leaf,
+                        int *first_child, int *nchild, float *com_mass);
+
+} // namespace nb
+
+// The simulation object behind nb_sim*.
+struct nb_sim {
+    nb_config cfg{};
+    size_t capacity = 0;
+    size_t n = 0;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+
+    // FP64 state: x y z vx vy vz ax ay az m, each `capacity` doubles.
+    nb::DevBuf state;
+    double *f[10] = {};
+    bool forces_valid = false;
+
+    nb::DevBuf split_hi, split_lo;   // float4 mirrors for the mixed kernel
+    nb::DevBuf partials;             // j-split partial sums
+    nb::DevBuf old_acc;              // velocity-Verlet a(t)
+    nb::DevBuf rk4;                  // RK4 stage states and accelerations
+    nb::DevBuf diag_scratch;
+    nb::BHTree *bh = nullptr;
+
+    // Optional timing of the dominant force kernel (nb_profile_*).
+    bool profiling = false;
+    std::vector<nb::KernelTimer> timers;
+    size_t timers_used = 0;
+
+    double *x() const { return f[0]; }
+    double *y() const { return f[1]; }
+    double *z() const { return f[2]; }
+    double *vx() const { return f[3]; }
+    double *vy() const { return f[4]; }
+    double *vz() const { return f[5]; }
+    double *ax() const { return f[6]; }
+    double *ay() const { return f[7]; }
+    double *az() const { return f[8]; }
+    double *m() const { return f[9]; }
+};
+
+namespace nb {
+// Evaluates accelerations of positions (px,py,pz) with masses m into out*.
+nb_status eval_forces(nb_sim *s, const double *px, const double *py, const double *pz,
+                      double *oax, double *oay, double *oaz);
+}

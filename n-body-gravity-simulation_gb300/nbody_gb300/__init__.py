@@ -1,0 +1,334 @@
+"""nbody_gb300 -- Python front end of the GB300 N-body engine.
+
+A thin ctypes layer over the C ABI in ``include/nbody_c.h`` (the library
+``libnbody_gb300.so`` next to this file).  The numerics all live in the CUDA
+kernels; this module only moves numpy arrays across the boundary.  It raises
+``NBodyError`` on every non-OK status and refuses to run when the library has
+not been built (there is no CPU fallback).
+
+    from nbody_gb300 import Sim, Config, DIRECT_MIXED, VELOCITY_VERLET
+    sim = Sim(Config(method=DIRECT_MIXED, G=1.0, softening=1e-3), capacity=n)
+    sim.load(x, y, z, vx, vy, vz, m)
+    sim.step(VELOCITY_VERLET, dt=5e-4, nsteps=10)
+    state = sim.read_state()
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnbody_gb300.so")
+COMPAT_LIB_PATH = os.path.join(HERE, "libnbody_compat.so")
+
+# nb_method
+DIRECT_FP64, DIRECT_MIXED, BARNES_HUT = 0, 1, 2
+# nb_integrator
+EULER, EULER_CROMER, LEAPFROG, VELOCITY_VERLET, RK4 = 0, 1, 2, 3, 4
+
+STATUS = {0: "NB_OK", 1: "NB_ERR_INVALID_ARGUMENT", 2: "NB_ERR_CUDA", 3: "NB_ERR_OUT_OF_MEMORY",
+          4: "NB_ERR_CAPACITY", 5: "NB_ERR_NOT_LOADED", 6: "NB_ERR_DEVICE_FAULT",
+          7: "NB_ERR_UNSUPPORTED"}
+
+# Every function declared in include/nbody_c.h (checked by the tests).
+EXPORTS = [
+    "nb_config_default", "nb_create", "nb_destroy", "nb_set_config", "nb_get_config",
+    "nb_load", "nb_load_device", "nb_read_state", "nb_device_arrays", "nb_num_bodies",
+    "nb_compute_forces", "nb_step", "nb_invalidate_forces", "nb_synchronize",
+    "nb_diagnostics", "nb_bh_build", "nb_bh_read_order", "nb_bh_read_nodes",
+    "nb_gen_plummer", "nb_gen_disk_bulge", "nb_status_string", "nb_last_error", "nb_version",
+    "nb_profile_enable", "nb_profile_read", "nb_kernel_launch_count",
+]
+_NON_STATUS = {"nb_status_string", "nb_last_error", "nb_version", "nb_kernel_launch_count"}
+
+
+class NBodyError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str):
+        super().__init__(f"{where}: {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class _Config(C.Structure):
+    _fields_ = [("method", C.c_int), ("G", C.c_double), ("softening", C.c_double),
+                ("theta", C.c_double), ("leaf_capacity", C.c_int), ("flags", C.c_int)]
+
+
+class _Diag(C.Structure):
+    _fields_ = [("kinetic", C.c_double), ("potential", C.c_double),
+                ("potential_softened", C.c_double), ("total", C.c_double),
+                ("total_softened", C.c_double), ("angular_momentum", C.c_double * 3),
+                ("center_of_mass", C.c_double * 3), ("momentum", C.c_double * 3),
+                ("mass", C.c_double)]
+
+
+class _BHInfo(C.Structure):
+    _fields_ = [("num_nodes", C.c_int), ("num_leaves", C.c_int), ("max_depth", C.c_int),
+                ("split_levels", C.c_int), ("root", C.c_double * 4)]
+
+
+class _Profile(C.Structure):
+    _fields_ = [("kernel_launches", C.c_uint64), ("force_launches", C.c_uint64),
+                ("force_kernel_ms", C.c_double)]
+
+
+def kernel_launch_count() -> int:
+    """This library's kernel launches in the process so far."""
+    return int(lib().nb_kernel_launch_count())
+
+
+@dataclass
+class Config:
+    method: int = DIRECT_MIXED
+    G: float = 1.0
+    softening: float = 0.0
+    theta: float = 0.5
+    leaf_capacity: int = 8
+    flags: int = 0
+
+    def _c(self) -> _Config:
+        return _Config(self.method, self.G, self.softening, self.theta, self.leaf_capacity,
+                       self.flags)
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def lib():
+    """Loads libnbody_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with "
+            "`python n-body-gravity-simulation_gb300/build.py` (no CPU fallback exists)")
+    L = C.CDLL(LIB_PATH)
+    vp, dp, sz = C.c_void_p, C.POINTER(C.c_double), C.c_size_t
+    L.nb_config_default.argtypes = [C.POINTER(_Config)]
+    L.nb_create.argtypes = [C.POINTER(_Config), sz, vp, C.POINTER(vp)]
+    L.nb_destroy.argtypes = [vp]
+    L.nb_set_config.argtypes = [vp, C.POINTER(_Config)]
+    L.nb_get_config.argtypes = [vp, C.POINTER(_Config)]
+    L.nb_load.argtypes = [vp, sz] + [vp] * 7
+    L.nb_load_device.argtypes = [vp, sz] + [vp] * 7
+    L.nb_read_state.argtypes = [vp] + [vp] * 10
+    L.nb_device_arrays.argtypes = [vp, C.POINTER(vp)]
+    L.nb_num_bodies.argtypes = [vp, C.POINTER(sz)]
+    L.nb_compute_forces.argtypes = [vp]
+    L.nb_step.argtypes = [vp, C.c_int, C.c_double, C.c_int]
+    L.nb_invalidate_forces.argtypes = [vp]
+    L.nb_synchronize.argtypes = [vp]
+    L.nb_diagnostics.argtypes = [vp, C.POINTER(_Diag)]
+    L.nb_bh_build.argtypes = [vp, C.POINTER(_BHInfo)]
+    L.nb_bh_read_order.argtypes = [vp, vp, vp]
+    L.nb_bh_read_nodes.argtypes = [vp, C.c_int] + [vp] * 8
+    L.nb_gen_plummer.argtypes = [sz, C.c_uint64, C.c_double, C.c_double, C.c_double] + [vp] * 7
+    L.nb_gen_disk_bulge.argtypes = ([sz, C.c_uint64] + [C.c_double] * 7 + [vp] * 7)
+    L.nb_status_string.argtypes = [C.c_int]
+    L.nb_status_string.restype = C.c_char_p
+    L.nb_last_error.restype = C.c_char_p
+    L.nb_version.restype = C.c_char_p
+    L.nb_profile_enable.argtypes = [vp, C.c_int]
+    L.nb_profile_read.argtypes = [vp, C.POINTER(_Profile), C.c_int]
+    L.nb_kernel_launch_count.restype = C.c_uint64
+    for name in EXPORTS:
+        f = getattr(L, name)
+        if name not in _NON_STATUS:
+            f.restype = C.c_int
+    _lib = L
+    return L
+
+
+def _check(status: int, where: str):
+    if status != 0:
+        msg = lib().nb_last_error().decode(errors="replace")
+        raise NBodyError(status, where, msg)
+
+
+def _ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+# ------------------------------------------------------------------ generators
+def plummer(n: int, seed: int = 0, total_mass: float = 1.0, scale: float = 1.0,
+            G: float = 1.0):
+    """Equal-mass Plummer sphere (Aarseth-Henon-Wielen); returns
+    (x, y, z, vx, vy, vz, m) as float64 arrays."""
+    out = [np.empty(n) for _ in range(7)]
+    _check(lib().nb_gen_plummer(n, seed, total_mass, scale, G, *map(_ptr, out)),
+           "nb_gen_plummer")
+    return tuple(out)
+
+
+def disk_bulge(n: int, seed: int = 0, total_mass: float = 1.0, bulge_frac: float = 0.2,
+               bulge_scale: float = 0.2, disk_scale: float = 1.0, disk_height: float = 0.05,
+               dispersion: float = 0.1, G: float = 1.0):
+    out = [np.empty(n) for _ in range(7)]
+    _check(lib().nb_gen_disk_bulge(n, seed, total_mass, bulge_frac, bulge_scale, disk_scale,
+                                   disk_height, dispersion, G, *map(_ptr, out)),
+           "nb_gen_disk_bulge")
+    return tuple(out)
+
+
+# ------------------------------------------------------------------ simulation
+class Sim:
+    """One simulation on the current CUDA device (nb_sim)."""
+
+    def __init__(self, config: Config | None = None, capacity: int = 1,
+                 stream: int | None = None):
+        self._h = C.c_void_p()
+        cfg = (config or Config())._c()
+        _check(lib().nb_create(C.byref(cfg), capacity, C.c_void_p(stream or 0),
+                               C.byref(self._h)), "nb_create")
+        self.capacity = capacity
+
+    def close(self):
+        if self._h:
+            lib().nb_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def config(self) -> Config:
+        c = _Config()
+        _check(lib().nb_get_config(self._h, C.byref(c)), "nb_get_config")
+        return Config(c.method, c.G, c.softening, c.theta, c.leaf_capacity, c.flags)
+
+    @config.setter
+    def config(self, cfg: Config):
+        c = cfg._c()
+        _check(lib().nb_set_config(self._h, C.byref(c)), "nb_set_config")
+
+    @property
+    def n(self) -> int:
+        v = C.c_size_t()
+        _check(lib().nb_num_bodies(self._h, C.byref(v)), "nb_num_bodies")
+        return v.value
+
+    def load(self, x, y, z, vx, vy, vz, m):
+        arrs = [_f64(a) for a in (x, y, z, vx, vy, vz, m)]
+        n = len(arrs[0])
+        if any(len(a) != n for a in arrs):
+            raise ValueError("arrays differ in length")
+        self._keep = arrs  # pageable sources stay alive until the copies ran
+        _check(lib().nb_load(self._h, n, *map(_ptr, arrs)), "nb_load")
+        _check(lib().nb_synchronize(self._h), "nb_synchronize")
+        self._keep = None
+
+    def load_pointers(self, n: int, ptrs, device: bool = False):
+        """Loads from raw addresses (host pinned or device) without copies on
+        the Python side; the caller keeps the memory alive until synchronize()."""
+        f = lib().nb_load_device if device else lib().nb_load
+        _check(f(self._h, n, *[C.c_void_p(p) for p in ptrs]), "nb_load")
+
+    def read_state(self):
+        n = self.n
+        out = [np.empty(n) for _ in range(10)]
+        _check(lib().nb_read_state(self._h, *map(_ptr, out)), "nb_read_state")
+        keys = ["x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "m"]
+        return dict(zip(keys, out))
+
+    def read_pointers(self, ptrs10):
+        """Copies the state into raw host addresses (None / 0 skips a field)."""
+        _check(lib().nb_read_state(self._h, *[C.c_void_p(p) if p else None for p in ptrs10]),
+               "nb_read_state")
+
+    def accelerations(self):
+        s = self.read_state()
+        return s["ax"], s["ay"], s["az"]
+
+    def device_arrays(self):
+        arr = (C.c_void_p * 10)()
+        _check(lib().nb_device_arrays(self._h, arr), "nb_device_arrays")
+        return [arr[k] for k in range(10)]
+
+    def compute_forces(self):
+        _check(lib().nb_compute_forces(self._h), "nb_compute_forces")
+
+    def step(self, integrator: int, dt: float, nsteps: int = 1):
+        _check(lib().nb_step(self._h, integrator, dt, nsteps), "nb_step")
+
+    def invalidate_forces(self):
+        _check(lib().nb_invalidate_forces(self._h), "nb_invalidate_forces")
+
+    def synchronize(self):
+        _check(lib().nb_synchronize(self._h), "nb_synchronize")
+
+    def diagnostics(self) -> dict:
+        d = _Diag()
+        _check(lib().nb_diagnostics(self._h, C.byref(d)), "nb_diagnostics")
+        return dict(kinetic=d.kinetic, potential=d.potential,
+                    potential_softened=d.potential_softened, total=d.total,
+                    total_softened=d.total_softened,
+                    angular_momentum=list(d.angular_momentum),
+                    center_of_mass=list(d.center_of_mass), momentum=list(d.momentum),
+                    mass=d.mass)
+
+    def profile(self, enable: bool = True):
+        _check(lib().nb_profile_enable(self._h, int(enable)), "nb_profile_enable")
+
+    def profile_read(self, reset: bool = True) -> dict:
+        p = _Profile()
+        _check(lib().nb_profile_read(self._h, C.byref(p), int(reset)), "nb_profile_read")
+        return dict(kernel_launches=p.kernel_launches, force_launches=p.force_launches,
+                    force_kernel_ms=p.force_kernel_ms)
+
+    # -------------------------------------------------------------- Barnes-Hut
+    def bh_build(self) -> dict:
+        info = _BHInfo()
+        _check(lib().nb_bh_build(self._h, C.byref(info)), "nb_bh_build")
+        return dict(num_nodes=info.num_nodes, num_leaves=info.num_leaves,
+                    max_depth=info.max_depth, split_levels=info.split_levels,
+                    root=list(info.root))
+
+    def bh_order(self):
+        n = self.n
+        codes = np.empty(n, np.uint64)
+        order = np.empty(n, np.uint32)
+        _check(lib().nb_bh_read_order(self._h, _ptr(codes), _ptr(order)), "nb_bh_read_order")
+        return codes, order
+
+    def bh_nodes(self, num_nodes: int) -> dict:
+        a = dict(depth=np.empty(num_nodes, np.int32), prefix=np.empty(num_nodes, np.uint64),
+                 first=np.empty(num_nodes, np.int32), count=np.empty(num_nodes, np.int32),
+                 is_leaf=np.empty(num_nodes, np.int32),
+                 first_child=np.empty(num_nodes, np.int32),
+                 nchild=np.empty(num_nodes, np.int32),
+                 com_mass=np.empty((num_nodes, 4), np.float32))
+        _check(lib().nb_bh_read_nodes(self._h, num_nodes, _ptr(a["depth"]), _ptr(a["prefix"]),
+                                      _ptr(a["first"]), _ptr(a["count"]), _ptr(a["is_leaf"]),
+                                      _ptr(a["first_child"]), _ptr(a["nchild"]),
+                                      _ptr(a["com_mass"])), "nb_bh_read_nodes")
+        return a
+
+
+def version() -> str:
+    return lib().nb_version().decode()
