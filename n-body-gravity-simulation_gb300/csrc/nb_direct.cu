@@ -9,9 +9,12 @@
 //    (xj_hi - xi_hi) + (xj_lo - xi_lo), which is exact to FP32 rounding for close
 //    pairs, so close encounters keep a relative force error near 1e-7 however far
 //    the pair is from the origin.  The rest of the pair term is plain FP32 on the
-//    FMA pipe with one MUFU rsqrt (rsqrt.approx.ftz.f32).  Every thread owns
+//    FMA pipe with one MUFU rsqrt (rsqrt.approx.ftz.f32) whose ~1.3e-7 error is
+//    removed by a Newton step folded into r^-3 (3 extra FP32 ops: 21 FP32-pipe
+//    operations + 1 MUFU per pair against the 12 of the bare pair term).  Every
+//    thread owns
 //    IPT i-bodies, so one broadcast shared-memory read of a j-body feeds IPT pair
-//    terms.  Per j-tile the FP32 tile sum is added into a Kahan-compensated
+//    terms.  Every 32 j the FP32 partial sum is added into a Kahan-compensated
 //    (sum, compensation) pair; the CTA's partial over its j-segment is written
 //    as FP32 (sum, comp) and the segments are combined in FP64.
 //    The tensor cores stay idle: a softened 1/r^3 sum is not a contraction.
@@ -92,12 +95,18 @@ direct_mixed_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo
         sh_lo[tid] = l;
         __syncthreads();
 
+        // FP32 partial sums over kSub consecutive j, Kahan-added into (s, c):
+        // the rounding of a running FP32 sum grows with its length, and 32
+        // terms keep it below the per-term error of the pair arithmetic.
+        constexpr int kSub = 32;
+#pragma unroll 1
+        for (int j0 = 0; j0 < BLOCK; j0 += kSub) {
         float ax[IPT], ay[IPT], az[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; ++k) ax[k] = ay[k] = az[k] = 0.f;
 
 #pragma unroll 4
-        for (int jj = 0; jj < BLOCK; ++jj) {
+        for (int jj = j0; jj < j0 + kSub; ++jj) {
             const float4 H = sh_hi[jj];
             const float4 L = sh_lo[jj];
 #pragma unroll
@@ -109,7 +118,12 @@ direct_mixed_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo
                 float inv = rsqrt_mufu(r2);
                 if (ZERO_SOFT) inv = (r2 > 0.f) ? inv : 0.f;  // the j == i term
                 const float inv2 = inv * inv;
-                const float s = (H.w * inv) * inv2;
+                // MUFU rsqrt is good to ~1.3e-7; y^3 with y = y0 (1 + d) is
+                // y0^3 (1 - 3d) to first order and r2 y0^2 = 1 + 2d, so
+                // y^3 ~= y0^3 (2.5 - 1.5 r2 y0^2): one Newton step folded
+                // into the cube (3 FP32 ops) leaves an O(d^2) error.
+                const float corr = fmaf(-1.5f, r2 * inv2, 2.5f);
+                const float s = ((H.w * inv) * inv2) * corr;
                 ax[k] = fmaf(dx, s, ax[k]);
                 ay[k] = fmaf(dy, s, ay[k]);
                 az[k] = fmaf(dz, s, az[k]);
@@ -120,6 +134,7 @@ direct_mixed_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo
             kahan_add(sx[k], cx[k], ax[k]);
             kahan_add(sy[k], cy[k], ay[k]);
             kahan_add(sz[k], cz[k], az[k]);
+        }
         }
     }
 

@@ -179,6 +179,29 @@ ORC_API void orc_forces_naive(int n, const double *x, const double *y, const dou
     }
 }
 
+/* Sum of the magnitudes of the pair terms, s_i = sum_{j != i} |G m_j r_ij| /
+ * (r_ij^2 + eps2)^(3/2): the scale of the rounding error of any finite-precision
+ * evaluation of a_i.  s_i / |a_i| is the condition number of body i's sum (not a
+ * reference quantity: used by the tests to state error bounds). */
+ORC_API void orc_forces_naive_abs(int n, const double *x, const double *y, const double *z,
+                                  const double *m, double G, double eps2, double *sabs,
+                                  int nthreads)
+{
+    orc_set_threads(nthreads);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        double s = 0.0;
+        for (int j = 0; j < n; ++j) {
+            if (i == j) continue;
+            double rx = x[j] - x[i], ry = y[j] - y[i], rz = z[j] - z[i];
+            double r2 = rx * rx + ry * ry + rz * rz;
+            double d2 = r2 + eps2;
+            s += G * m[j] * sqrt(r2) / (d2 * sqrt(d2));
+        }
+        sabs[i] = s;
+    }
+}
+
 /* Rows [i0, i1) of the direct sum (the bounded CPU-baseline sample). */
 ORC_API void orc_forces_naive_rows(int n, int i0, int i1, const double *x, const double *y,
                                    const double *z, const double *m, double G, double eps2,

@@ -55,6 +55,8 @@ def lib():
         L.orc_gen_uniform_cube.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _dp]
         L.orc_forces_naive.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_double, C.c_double,
                                        _dp, _dp, _dp, C.c_int]
+        L.orc_forces_naive_abs.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_double,
+                                           C.c_double, _dp, C.c_int]
         L.orc_forces_naive_rows.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
                                             C.c_double, C.c_double, _dp, _dp, _dp, C.c_int]
         L.orc_forces_bh_opt.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_double, C.c_double,
@@ -143,6 +145,14 @@ def forces_naive(x, y, z, m, G, eps, nthreads=0):
     ax, ay, az = np.empty(n), np.empty(n), np.empty(n)
     lib().orc_forces_naive(n, x, y, z, m, G, eps * eps, ax, ay, az, nthreads)
     return ax, ay, az
+
+
+def forces_abs_sum(x, y, z, m, G, eps, nthreads=0):
+    """Per body sum_j |pair term| (the error scale of any FP evaluation)."""
+    x, y, z, m = map(_c, (x, y, z, m))
+    out = np.empty(len(x))
+    lib().orc_forces_naive_abs(len(x), x, y, z, m, G, eps * eps, out, nthreads)
+    return out
 
 
 def forces_naive_rows(x, y, z, m, G, eps, i0, i1, nthreads=0):
