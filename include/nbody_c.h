@@ -211,6 +211,27 @@ nb_status nb_gen_disk_bulge(size_t n, uint64_t seed, double total_mass, double b
                             double dispersion, double G, double *x, double *y, double *z,
                             double *vx, double *vy, double *vz, double *m);
 
+/* ---- all-pairs forces without device allocation ----------------------------- */
+
+/* No counterpart in the reference: an addition of this library for callers
+ * that may not allocate device memory (a host whose device memory is owned by
+ * its own pool allocator, a plugin with a fixed device-memory budget, a loop
+ * that cannot take the implicit synchronisation of cudaMalloc/cudaFree).
+ * Computes G-scaled accelerations of n bodies exactly as the NB_DIRECT_MIXED
+ * method does, from caller-owned DEVICE arrays x, y, z, m into caller-owned
+ * DEVICE arrays ax, ay, az, on `stream` (NULL = legacy default stream),
+ * asynchronously.  It allocates nothing: its scratch is one 16 MiB array in
+ * the library's device memory, present on every device that loads the
+ * library until the process exits, which limits n to 262144 (larger n returns
+ * NB_ERR_CAPACITY).  The first call on each device looks up that array's
+ * device address (cudaGetSymbolAddress) and must run with that device current
+ * and before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU race and must be serialised by the caller. */
+nb_status nb_direct_mixed_forces_noalloc(size_t n, const double *x, const double *y,
+                                         const double *z, const double *m, double G,
+                                         double softening, double *ax, double *ay, double *az,
+                                         void *stream);
+
 /* ---- measurement ---------------------------------------------------------- */
 
 /* Device time of the dominant force kernel (the all-pairs kernel or the tree

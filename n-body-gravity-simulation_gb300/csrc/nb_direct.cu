@@ -28,6 +28,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <string>
 
 namespace nb {
 namespace {
@@ -393,3 +395,114 @@ nb_status direct_fp64(const double *x, const double *y, const double *z, const d
 }
 
 } // namespace nb
+
+// ---------------------------------------------------------------------------
+// All-pairs forces for callers that cannot allocate device memory.
+//
+// Some callers of this library may not call cudaMalloc/cudaFree on their hot
+// path: a host application whose device memory is entirely owned by its own
+// pool allocator, a plugin that is given a fixed device-memory budget at
+// start-up, or a real-time loop that cannot afford the implicit device-wide
+// synchronisation an allocation or free can cause.  For them,
+// nb_direct_mixed_forces_noalloc runs the same split / all-pairs / combine
+// kernels as the NB_DIRECT_MIXED method, but keeps its scratch (the float4
+// hi/lo mirror of the bodies and the per-segment Kahan partial sums) in the
+// file-scope device array below instead of memory it allocates.
+//
+// The array is kNoAllocScratchBytes (16 MiB) on every device that loads this
+// library, held until the process exits, and limits n to kNoAllocMaxBodies.
+// Its name is only a host-side stand-in in host code: the device address is
+// fetched once per device with cudaGetSymbolAddress, by the first call made
+// while that device is current (make that first call before any stream
+// capture).  Every call shares the one array and leaves its contents behind;
+// no part of it has to start at zero, because each call writes every element
+// it later reads.  Calls whose kernels overlap on the GPU (different streams,
+// or another thread) race on the array and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+static constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace nb {
+namespace {
+
+constexpr size_t kNoAllocMaxBodies = 262144;  // hi/lo (32 B) + one segment (24 B) per body
+constexpr int kNoAllocMaxDevices = 64;
+
+std::mutex g_noalloc_mutex;
+void *g_noalloc_address[kNoAllocMaxDevices] = {};
+
+size_t round_up_256(size_t b) { return (b + 255) / 256 * 256; }
+
+} // namespace
+} // namespace nb
+
+extern "C" nb_status nb_direct_mixed_forces_noalloc(size_t n, const double *x, const double *y,
+                                                   const double *z, const double *m, double G,
+                                                   double softening, double *ax, double *ay,
+                                                   double *az, void *stream)
+{
+    using namespace nb;
+    if (n > kNoAllocMaxBodies)
+        return fail(NB_ERR_CAPACITY,
+                    "nb_direct_mixed_forces_noalloc: n = " + std::to_string(n) +
+                        " exceeds its fixed scratch limit of " +
+                        std::to_string(kNoAllocMaxBodies) + " bodies");
+    if (n == 0) return NB_OK;
+    if (!x || !y || !z || !m || !ax || !ay || !az)
+        return fail(NB_ERR_INVALID_ARGUMENT, "nb_direct_mixed_forces_noalloc: NULL array");
+    if (!(softening >= 0.0))
+        return fail(NB_ERR_INVALID_ARGUMENT, "nb_direct_mixed_forces_noalloc: softening < 0");
+    int dev = 0;
+    NB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return fail(NB_ERR_UNSUPPORTED, "nb_direct_mixed_forces_noalloc: device ordinal >= 64");
+    void *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_address[dev]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
+            g_noalloc_address[dev] = p;
+        }
+        base = g_noalloc_address[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int ni = (int)n;
+    const size_t mirror = round_up_256(sizeof(float4) * n);
+    float4 *hi = static_cast<float4 *>(base);
+    float4 *lo = reinterpret_cast<float4 *>(static_cast<unsigned char *>(base) + mirror);
+    float *psum = reinterpret_cast<float *>(static_cast<unsigned char *>(base) + 2 * mirror);
+
+    // Same plan as the allocating path, with the j-split capped so that the
+    // partial sums fit the remaining scratch.
+    DirectPlan p = direct_mixed_plan(ni);
+    const int tiles = (ni + p.block - 1) / p.block;
+    const size_t per_segment = sizeof(float) * 6 * n;
+    const int max_segments = (int)std::max<size_t>(1, (kNoAllocScratchBytes - 2 * mirror) /
+                                                          per_segment);
+    if (p.segments > max_segments) {
+        p.seg_tiles = (tiles + max_segments - 1) / max_segments;
+        p.segments = (tiles + p.seg_tiles - 1) / p.seg_tiles;
+    }
+    float *pcomp = psum + 3 * n * (size_t)p.segments;
+
+    split_kernel<<<(ni + 255) / 256, 256, 0, st>>>(x, y, z, m, ni, hi, lo);
+    NB_LAUNCH_CHECK();
+    const double eps2 = softening * softening;
+    const int per_cta = p.block * p.ipt;
+    dim3 grid((ni + per_cta - 1) / per_cta, p.segments);
+    const int seg_len = p.seg_tiles * p.block;
+    if (eps2 > 0.0)
+        direct_mixed_kernel<kMixBlock, kMixIpt, false>
+            <<<grid, kMixBlock, 0, st>>>(hi, lo, ni, (float)eps2, seg_len, psum, pcomp);
+    else
+        direct_mixed_kernel<kMixBlock, kMixIpt, true>
+            <<<grid, kMixBlock, 0, st>>>(hi, lo, ni, 0.0f, seg_len, psum, pcomp);
+    NB_LAUNCH_CHECK();
+    combine_mixed_kernel<<<(ni + 255) / 256, 256, 0, st>>>(psum, pcomp, ni, p.segments, G, ax,
+                                                          ay, az);
+    NB_LAUNCH_CHECK();
+    return NB_OK;
+}

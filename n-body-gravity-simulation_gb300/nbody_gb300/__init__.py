@@ -41,6 +41,7 @@ EXPORTS = [
     "nb_diagnostics", "nb_bh_build", "nb_bh_read_order", "nb_bh_read_nodes",
     "nb_gen_plummer", "nb_gen_disk_bulge", "nb_status_string", "nb_last_error", "nb_version",
     "nb_profile_enable", "nb_profile_read", "nb_kernel_launch_count",
+    "nb_direct_mixed_forces_noalloc",
 ]
 _NON_STATUS = {"nb_status_string", "nb_last_error", "nb_version", "nb_kernel_launch_count"}
 
@@ -138,6 +139,8 @@ def lib():
     L.nb_profile_enable.argtypes = [vp, C.c_int]
     L.nb_profile_read.argtypes = [vp, C.POINTER(_Profile), C.c_int]
     L.nb_kernel_launch_count.restype = C.c_uint64
+    L.nb_direct_mixed_forces_noalloc.argtypes = ([sz] + [vp] * 4 + [C.c_double] * 2 +
+                                                 [vp] * 3 + [vp])
     for name in EXPORTS:
         f = getattr(L, name)
         if name not in _NON_STATUS:
