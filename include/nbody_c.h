@@ -175,23 +175,30 @@ typedef struct nb_bh_info {
     int max_depth;
     int split_levels;   /* levels the root cube may split (<= 21) */
     double root[4];     /* centre x, y, z and side of the root cube */
+    uint64_t interactions_m2p;  /* body-node (monopole) terms of the last walk */
+    uint64_t interactions_p2p;  /* body-body terms of the last walk (self included) */
 } nb_bh_info;
 
 /* Builds the tree of the current positions (without a walk) and reports it. */
 nb_status nb_bh_build(nb_sim *sim, nb_bh_info *info);
+
+/* Reports the tree and the interaction counts of the last Barnes-Hut force
+ * evaluation (the reference prints build/walk times only). */
+nb_status nb_bh_get_info(nb_sim *sim, nb_bh_info *info);
 
 /* After nb_bh_build or a Barnes-Hut force evaluation: the sorted 63-bit
  * Morton codes and the original index of each sorted body (host arrays of
  * n entries; either may be NULL). */
 nb_status nb_bh_read_order(nb_sim *sim, uint64_t *sorted_codes, uint32_t *order);
 
-/* Node table in breadth-first order (host arrays of max_nodes entries; any
- * may be NULL): depth, Morton prefix, first sorted body, body count, leaf
- * flag, first child, child count; com_mass gets 4 floats per node (COM xyz,
- * mass).  Returns NB_ERR_CAPACITY when max_nodes is too small. */
+/* Node table in depth-first preorder, children in Morton order (host arrays
+ * of max_nodes entries; any may be NULL): depth, Morton prefix (top 3*depth
+ * bits), first sorted body, body count, leaf flag, skip (index of the next
+ * node outside the subtree; the first child of an internal node is the next
+ * index); com_mass gets 4 floats per node (COM xyz, mass).  Returns
+ * NB_ERR_CAPACITY when max_nodes is smaller than the node count. */
 nb_status nb_bh_read_nodes(nb_sim *sim, int max_nodes, int *depth, uint64_t *prefix,
-                           int *first, int *count, int *is_leaf, int *first_child,
-                           int *nchild, float *com_mass);
+                           int *first, int *count, int *is_leaf, int *skip, float *com_mass);
 
 /* ---- host-side input generators (no GPU needed) ------------------------- */
 

@@ -132,8 +132,8 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
 nb_status bh_info(BHTree *t, cudaStream_t st, nb_bh_info *info);
 nb_status bh_read_order(BHTree *t, cudaStream_t st, uint64_t *codes, uint32_t *order);
 nb_status bh_read_nodes(BHTree *t, cudaStream_t st, int max_nodes, int *depth,
-                        uint64_t *prefix, int *first, int *count, int *is_leaf,
-                        int *first_child, int *nchild, float *com_mass);
+                        uint64_t *prefix, int *first, int *count, int *is_leaf, int *skip,
+                        float *com_mass);
 
 } // namespace nb
 

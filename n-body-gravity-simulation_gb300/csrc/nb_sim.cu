@@ -408,6 +408,13 @@ nb_status nb_bh_build(nb_sim *s, nb_bh_info *info)
     return NB_OK;
 }
 
+nb_status nb_bh_get_info(nb_sim *s, nb_bh_info *info)
+{
+    if (!s || !info) return fail(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!s->bh) return fail(NB_ERR_NOT_LOADED, "no Barnes-Hut tree built");
+    return bh_info(s->bh, s->stream, info);
+}
+
 nb_status nb_bh_read_order(nb_sim *s, uint64_t *codes, uint32_t *order)
 {
     if (!s) return fail(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
@@ -416,13 +423,12 @@ nb_status nb_bh_read_order(nb_sim *s, uint64_t *codes, uint32_t *order)
 }
 
 nb_status nb_bh_read_nodes(nb_sim *s, int max_nodes, int *depth, uint64_t *prefix, int *first,
-                           int *count, int *is_leaf, int *first_child, int *nchild,
-                           float *com_mass)
+                           int *count, int *is_leaf, int *skip, float *com_mass)
 {
     if (!s) return fail(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
     if (!s->bh) return fail(NB_ERR_NOT_LOADED, "no Barnes-Hut tree built");
     return bh_read_nodes(s->bh, s->stream, max_nodes, depth, prefix, first, count, is_leaf,
-                         first_child, nchild, com_mass);
+                         skip, com_mass);
 }
 
 nb_status nb_profile_enable(nb_sim *s, int enable)

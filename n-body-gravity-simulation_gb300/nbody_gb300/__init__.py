@@ -38,7 +38,7 @@ EXPORTS = [
     "nb_config_default", "nb_create", "nb_destroy", "nb_set_config", "nb_get_config",
     "nb_load", "nb_load_device", "nb_read_state", "nb_device_arrays", "nb_num_bodies",
     "nb_compute_forces", "nb_step", "nb_invalidate_forces", "nb_synchronize",
-    "nb_diagnostics", "nb_bh_build", "nb_bh_read_order", "nb_bh_read_nodes",
+    "nb_diagnostics", "nb_bh_build", "nb_bh_get_info", "nb_bh_read_order", "nb_bh_read_nodes",
     "nb_gen_plummer", "nb_gen_disk_bulge", "nb_status_string", "nb_last_error", "nb_version",
     "nb_profile_enable", "nb_profile_read", "nb_kernel_launch_count",
     "nb_direct_mixed_forces_noalloc",
@@ -67,7 +67,8 @@ class _Diag(C.Structure):
 
 class _BHInfo(C.Structure):
     _fields_ = [("num_nodes", C.c_int), ("num_leaves", C.c_int), ("max_depth", C.c_int),
-                ("split_levels", C.c_int), ("root", C.c_double * 4)]
+                ("split_levels", C.c_int), ("root", C.c_double * 4),
+                ("interactions_m2p", C.c_uint64), ("interactions_p2p", C.c_uint64)]
 
 
 class _Profile(C.Structure):
@@ -128,8 +129,9 @@ def lib():
     L.nb_synchronize.argtypes = [vp]
     L.nb_diagnostics.argtypes = [vp, C.POINTER(_Diag)]
     L.nb_bh_build.argtypes = [vp, C.POINTER(_BHInfo)]
+    L.nb_bh_get_info.argtypes = [vp, C.POINTER(_BHInfo)]
     L.nb_bh_read_order.argtypes = [vp, vp, vp]
-    L.nb_bh_read_nodes.argtypes = [vp, C.c_int] + [vp] * 8
+    L.nb_bh_read_nodes.argtypes = [vp, C.c_int] + [vp] * 7
     L.nb_gen_plummer.argtypes = [sz, C.c_uint64, C.c_double, C.c_double, C.c_double] + [vp] * 7
     L.nb_gen_disk_bulge.argtypes = ([sz, C.c_uint64] + [C.c_double] * 7 + [vp] * 7)
     L.nb_status_string.argtypes = [C.c_int]
@@ -306,11 +308,16 @@ class Sim:
 
     # -------------------------------------------------------------- Barnes-Hut
     def bh_build(self) -> dict:
+        """Builds the tree of the current positions (no walk) and reports it."""
         info = _BHInfo()
         _check(lib().nb_bh_build(self._h, C.byref(info)), "nb_bh_build")
-        return dict(num_nodes=info.num_nodes, num_leaves=info.num_leaves,
-                    max_depth=info.max_depth, split_levels=info.split_levels,
-                    root=list(info.root))
+        return _bh_info_dict(info)
+
+    def bh_info(self) -> dict:
+        """The last tree and walk (after a Barnes-Hut force evaluation)."""
+        info = _BHInfo()
+        _check(lib().nb_bh_get_info(self._h, C.byref(info)), "nb_bh_get_info")
+        return _bh_info_dict(info)
 
     def bh_order(self):
         n = self.n
@@ -320,17 +327,23 @@ class Sim:
         return codes, order
 
     def bh_nodes(self, num_nodes: int) -> dict:
+        """Node table (depth-first preorder) of the last tree."""
         a = dict(depth=np.empty(num_nodes, np.int32), prefix=np.empty(num_nodes, np.uint64),
                  first=np.empty(num_nodes, np.int32), count=np.empty(num_nodes, np.int32),
-                 is_leaf=np.empty(num_nodes, np.int32),
-                 first_child=np.empty(num_nodes, np.int32),
-                 nchild=np.empty(num_nodes, np.int32),
+                 is_leaf=np.empty(num_nodes, np.int32), skip=np.empty(num_nodes, np.int32),
                  com_mass=np.empty((num_nodes, 4), np.float32))
         _check(lib().nb_bh_read_nodes(self._h, num_nodes, _ptr(a["depth"]), _ptr(a["prefix"]),
                                       _ptr(a["first"]), _ptr(a["count"]), _ptr(a["is_leaf"]),
-                                      _ptr(a["first_child"]), _ptr(a["nchild"]),
-                                      _ptr(a["com_mass"])), "nb_bh_read_nodes")
+                                      _ptr(a["skip"]), _ptr(a["com_mass"])),
+               "nb_bh_read_nodes")
         return a
+
+
+def _bh_info_dict(info) -> dict:
+    return dict(num_nodes=info.num_nodes, num_leaves=info.num_leaves,
+                max_depth=info.max_depth, split_levels=info.split_levels,
+                root=list(info.root), interactions_m2p=info.interactions_m2p,
+                interactions_p2p=info.interactions_p2p)
 
 
 def version() -> str:

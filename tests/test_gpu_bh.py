@@ -1,0 +1,248 @@
+"""GPU Barnes-Hut against the CPU oracle.
+
+Bit-exact (integers):
+  - the 63-bit Morton codes and the stable sort order equal the oracle's
+    restatement (oracle/nbody_oracle.c section 7) of the CPU tree's cell
+    comparisons;
+  - the octree (depth, Morton prefix, first body, body count, leaf flag of
+    every node) equals the oracle's octree over the sorted codes, which
+    tests/test_oracle.py shows is the reference CPU node-pool tree's set of
+    non-empty cells; skip pointers follow depth-first preorder.
+Within tolerance (floating point):
+  - node masses to 1e-12 (FP64 prefix sums) and centres of mass to FP32
+    rounding of the system size;
+  - forces vs the FP64 direct sum inside the reference's own Barnes-Hut
+    accuracy envelope at theta = 0.5 (CUDA/outputs/output1_2.txt and
+    CPU/outputs/output2_4.txt: mean relative error 2.8e-3 at N = 10,000);
+    the warp-cooperative walk opens every node any body of the warp opens, so
+    it must be at least as accurate as the CPU node-pool tree on the same
+    input.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def cube(oracle, n, seed=42, order=1):
+    g = oracle.MT19937(seed)
+    x, y, z, m = g.uniform_cube(n, order=order)
+    zero = np.zeros(n)
+    return x, y, z, zero, zero.copy(), zero.copy(), m
+
+
+def bh_sim(nb, state, G=1.0, eps=0.0, theta=0.5, leaf=8):
+    n = len(state[0])
+    s = nb.Sim(nb.Config(method=nb.BARNES_HUT, G=G, softening=eps, theta=theta,
+                         leaf_capacity=leaf), capacity=n)
+    s.load(*state)
+    return s
+
+
+def oracle_tree(oracle, x, y, z, leaf):
+    codes, root = oracle.morton63(x, y, z)
+    sc, order = oracle.sort_codes(codes)
+    levels = oracle.split_levels(root[3])
+    return sc, order, oracle.octree(sc, leaf, levels), root, levels
+
+
+def check_preorder(nodes):
+    """Skip pointers and first-child order of a depth-first preorder table."""
+    nn = len(nodes["depth"])
+    depth, skip, first, count = nodes["depth"], nodes["skip"], nodes["first"], nodes["count"]
+    leaf = nodes["is_leaf"].astype(bool)
+    assert skip[0] == nn
+    for v in range(nn):
+        assert v < skip[v] <= nn
+        if not leaf[v]:
+            # children: v+1, skip(v+1), ... up to skip(v); they tile the parent's range
+            c, pos, total = v + 1, first[v], 0
+            while c < skip[v]:
+                assert depth[c] == depth[v] + 1
+                assert first[c] == pos
+                pos += count[c]
+                total += count[c]
+                c = skip[c]
+            assert c == skip[v] and total == count[v]
+        else:
+            assert skip[v] == v + 1
+
+
+WORKLOADS = ["cube5000", "plummer20000", "diskbulge20000", "cube_leaf1_3000", "clustered"]
+
+
+def make(nb, oracle, name):
+    if name == "cube5000":
+        return cube(oracle, 5000), 8
+    if name == "plummer20000":
+        return nb.plummer(20000, seed=3), 8
+    if name == "diskbulge20000":
+        return nb.disk_bulge(20000, seed=4), 8
+    if name == "cube_leaf1_3000":
+        return cube(oracle, 3000, seed=7), 1
+    # two tight clumps plus duplicates: deep chains and unsplittable cells
+    rng = np.random.default_rng(5)
+    a = rng.normal(size=(2000, 3)) * 1e-6
+    b = rng.normal(size=(2000, 3)) * 1e-6 + 1.0
+    p = np.concatenate([a, b, np.zeros((20, 3))])
+    n = len(p)
+    return (p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy(), np.zeros(n), np.zeros(n),
+            np.zeros(n), np.full(n, 1.0 / n)), 4
+
+
+@pytest.mark.parametrize("name", WORKLOADS)
+def test_codes_order_and_topology_bit_exact(nb, oracle, name):
+    state, leaf = make(nb, oracle, name)
+    x, y, z = state[0], state[1], state[2]
+    sc, order, t, root, levels = oracle_tree(oracle, x, y, z, leaf)
+    with bh_sim(nb, state, leaf=leaf) as s:
+        info = s.bh_build()
+        codes, gorder = s.bh_order()
+        assert info["split_levels"] == levels
+        assert info["root"] == list(root)
+        assert np.array_equal(codes, sc)
+        assert np.array_equal(gorder, order)
+        nodes = s.bh_nodes(info["num_nodes"])
+    assert info["num_nodes"] == len(t["depth"])
+    assert info["num_leaves"] == int(t["is_leaf"].sum())
+    got = sorted(zip(nodes["depth"].tolist(), nodes["prefix"].tolist(), nodes["first"].tolist(),
+                     nodes["count"].tolist(), nodes["is_leaf"].tolist()))
+    want = sorted(zip(t["depth"].tolist(), t["prefix"].tolist(), t["first"].tolist(),
+                      t["count"].tolist(), t["is_leaf"].tolist()))
+    assert got == want
+    check_preorder(nodes)
+
+
+def test_node_monopoles(nb, oracle):
+    state = nb.plummer(8000, seed=9)
+    x, y, z, m = state[0], state[1], state[2], state[6]
+    sc, order, t, root, levels = oracle_tree(oracle, x, y, z, 8)
+    with bh_sim(nb, state) as s:
+        info = s.bh_build()
+        nodes = s.bh_nodes(info["num_nodes"])
+    xs, ys, zs, ms = x[order], y[order], z[order], m[order]
+    size = root[3]
+    for v in range(0, info["num_nodes"], 7):
+        a, c = nodes["first"][v], nodes["count"][v]
+        M = ms[a:a + c].sum()
+        com = np.array([(ms[a:a + c] * xs[a:a + c]).sum(), (ms[a:a + c] * ys[a:a + c]).sum(),
+                        (ms[a:a + c] * zs[a:a + c]).sum()]) / M
+        assert nodes["com_mass"][v, 3] == pytest.approx(M, rel=1e-6)
+        assert np.abs(nodes["com_mass"][v, :3] - com).max() <= 1e-6 * size
+
+
+def _errors(a, ref):
+    d = np.sqrt(sum((u - v) ** 2 for u, v in zip(a, ref)))
+    r = np.sqrt(sum(v * v for v in ref))
+    mask = r > 1e-12
+    rel = d[mask] / r[mask]
+    return float(rel.sum() / len(d)), float(rel.max())
+
+
+def test_force_envelope_seed42_n10000(nb, oracle):
+    """The reference's CUDA benchmark input (x, y, z, mass draw order), N =
+    10,000, G = 4 pi^2, no softening, theta 0.5, leaf 8."""
+    fx = json.load(open(os.path.join(GOLDEN, "cuda_bh_envelope.json")))
+    ref_case = [c for c in fx["cases"] if c["n"] == 10000][0]
+    g = oracle.MT19937(42)
+    for n in (100, 500, 1000, 5000):  # the CUDA benchmark's earlier sizes share the rng
+        g.uniform_cube(n, order=1)
+    x, y, z, m = g.uniform_cube(10000, order=1)
+    zero = np.zeros(10000)
+    G = oracle.G_REF
+    with bh_sim(nb, (x, y, z, zero, zero, zero, m), G=G) as s:
+        s.compute_forces()
+        a = s.accelerations()
+    ref = oracle.forces_naive(x, y, z, m, G, 0.0)
+    cpu_bh = oracle.forces_bh_opt(x, y, z, m, G, 0.0, 0.5, 8)
+    avg, mx = _errors(a, ref)
+    cavg, cmx = _errors(cpu_bh, ref)
+    assert avg <= ref_case["avg_rel"], (avg, ref_case)
+    assert avg <= cavg, (avg, cavg)
+    assert mx <= max(ref_case["max_rel"], cmx), (mx, ref_case, cmx)
+
+
+@pytest.mark.parametrize("theta", [0.3, 0.6, 1.0])
+def test_force_accuracy_plummer(nb, oracle, theta):
+    state = nb.plummer(16384, seed=2)
+    x, y, z, m = state[0], state[1], state[2], state[6]
+    with bh_sim(nb, state, eps=1e-3, theta=theta) as s:
+        s.compute_forces()
+        a = s.accelerations()
+    ref = oracle.forces_naive(x, y, z, m, 1.0, 1e-3)
+    cpu_bh = oracle.forces_bh_opt(x, y, z, m, 1.0, 1e-3, theta, 8)
+    avg, mx = _errors(a, ref)
+    cavg, cmx = _errors(cpu_bh, ref)
+    assert avg <= 1.05 * cavg + 2e-6, (theta, avg, cavg)
+    assert mx <= 1.5 * cmx + 1e-5, (theta, mx, cmx)
+
+
+def test_theta_zero_is_direct_sum(nb, oracle):
+    """theta = 0 opens every node: the walk degenerates to the direct sum
+    (plain FP32 pair arithmetic and accumulation, as the reference's walk,
+    force_calculator_barnes_hut.cu:46-53)."""
+    state = nb.plummer(3000, seed=8)
+    x, y, z, m = state[0], state[1], state[2], state[6]
+    with bh_sim(nb, state, eps=1e-2, theta=0.0) as s:
+        s.compute_forces()
+        a = s.accelerations()
+        info = s.bh_info()
+    ref = oracle.forces_naive(x, y, z, m, 1.0, 1e-2)
+    avg, mx = _errors(a, ref)
+    assert mx < 2e-4 and avg < 1e-5, (mx, avg)
+    assert info["interactions_m2p"] == 0
+    assert info["interactions_p2p"] == 3000 * 3000
+
+
+@pytest.mark.parametrize("n", [1, 2, 8, 9, 33])
+def test_small_systems(nb, oracle, n):
+    state = cube(oracle, n, seed=100 + n)
+    x, y, z, m = state[0], state[1], state[2], state[6]
+    with bh_sim(nb, state, eps=0.1) as s:
+        s.compute_forces()
+        a = s.accelerations()
+    ref = oracle.forces_naive(x, y, z, m, 1.0, 0.1)
+    if n == 1:
+        assert all(v[0] == 0.0 for v in a)
+    else:
+        avg, mx = _errors(a, ref)
+        assert mx < 0.05
+
+
+def test_coincident_bodies_unsplittable_root(nb, oracle):
+    n = 50
+    x = np.full(n, 3.0); y = np.full(n, -1.0); z = np.full(n, 2.0)
+    zero = np.zeros(n)
+    with bh_sim(nb, (x, y, z, zero, zero, zero, np.ones(n)), eps=0.1) as s:
+        info = s.bh_build()
+        assert info["split_levels"] == 0 and info["num_nodes"] == 1
+        s.compute_forces()
+        a = s.accelerations()
+    assert all(np.array_equal(v, zero) for v in a)
+
+
+def test_deterministic(nb, oracle):
+    state = nb.disk_bulge(30000, seed=6)
+    out = []
+    for _ in range(2):
+        with bh_sim(nb, state, eps=1e-3) as s:
+            s.compute_forces()
+            out.append(s.accelerations())
+    for u, v in zip(*out):
+        assert np.array_equal(u, v)
+
+
+def test_leapfrog_energy(nb):
+    """Barnes-Hut leapfrog on a softened Plummer sphere conserves energy to
+    the force error."""
+    state = nb.plummer(8192, seed=1)
+    with bh_sim(nb, state, eps=0.01, theta=0.5) as s:
+        e0 = s.diagnostics()["total_softened"]
+        s.step(nb.LEAPFROG, 1e-3, 50)
+        e1 = s.diagnostics()["total_softened"]
+    assert abs(e1 - e0) / abs(e0) < 1e-4
