@@ -55,6 +55,9 @@ def parse():
                     help="target CPU time of the cpu_baseline sample")
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the headline value (no FP64 / accuracy / energy extras)")
+    ap.add_argument("--bh-steps", type=int, default=20,
+                    help="leapfrog steps of the Barnes-Hut N=2^20 extra (0 skips it)")
+    ap.add_argument("--bh-n", type=int, default=1 << 20)
     return ap.parse_args()
 
 
@@ -139,6 +142,21 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
+def profiled_traffic(name: str):
+    """DRAM bytes per launch from an ncu summary in profiles/ (the
+    `dram_bytes_per_launch:` line), or None."""
+    p = os.path.join(REPO, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return int(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
 def fp32_roofline_gint(num_sms: int, mhz: float) -> float:
     """All-pairs roofline: 12 FP32-pipe operations per interaction (3 FADD for
     the displacement, 3 FFMA for r^2, 3 FMUL for m r^-3, 3 FFMA to accumulate)
@@ -198,6 +216,72 @@ def run_reference(a, rank, world):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+# ---------------------------------------------------------------- Barnes-Hut
+BH_N = 1 << 20
+BH_THETA = 0.5
+BH_DT = 1e-3
+
+
+def run_bh(a, nb, torch, dev, stream, flush, np):
+    """The Barnes-Hut configuration: N = 2^20 bulge (Plummer, 20% of the mass,
+    scale 0.2) + exponential disk (scale length 1, height 0.05, circular
+    velocities + 0.1 dispersion), 63-bit Morton octree, theta 0.5, eps 1e-3,
+    FP32 walk / FP64 integration, leapfrog dt = 1e-3.  Reports steps/s over
+    a.bh_steps leapfrog steps (CUDA events per step, L2 flushed before each),
+    the walk kernel's share and rate, and the force error against the mixed
+    direct sum on a sample of bodies."""
+    n = a.bh_n
+    state = nb.disk_bulge(n, seed=SEED)
+    cfg = nb.Config(method=nb.BARNES_HUT, G=1.0, softening=EPS, theta=BH_THETA, leaf_capacity=8)
+    sim = nb.Sim(cfg, capacity=n, stream=stream.cuda_stream)
+    sim.load(*state)
+    for _ in range(3):
+        sim.step(nb.LEAPFROG, BH_DT, 1)
+    torch.cuda.synchronize()
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(a.bh_steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(a.bh_steps)]
+    sim.profile(True)
+    sim.profile_read(reset=True)
+    for k in range(a.bh_steps):
+        flush.zero_()
+        ev0[k].record(stream)
+        sim.step(nb.LEAPFROG, BH_DT, 1)
+        ev1[k].record(stream)
+    torch.cuda.synchronize()
+    prof = sim.profile_read(reset=True)
+    sim.profile(False)
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in zip(ev0, ev1)]
+    info = sim.bh_info()
+    inter = info["interactions_m2p"] + info["interactions_p2p"]
+    walk_ms = prof["force_kernel_ms"] / max(1, prof["force_launches"])
+    ms = sum(step_ms) / len(step_ms)
+    out = {"workload": f"disk_bulge_n{n}_theta{BH_THETA}_leapfrog", "n": n,
+           "steps": a.bh_steps, "ms_per_step": ms, "steps_per_s": 1e3 / ms,
+           "walk_ms": walk_ms, "walk_share": walk_ms / ms,
+           "interactions_per_body": inter / n,
+           "walk_ginteractions_s": inter / (walk_ms / 1e3) / 1e9,
+           "nodes": info["num_nodes"], "leaves": info["num_leaves"],
+           "max_depth": info["max_depth"], "timing": "CUDA events per leapfrog step, L2 "
+                                                     "flushed before each; includes one host "
+                                                     "read of the node count per step"}
+    # accuracy vs the mixed direct sum (itself within ~1e-6 of FP64)
+    st = sim.read_state()
+    bh_acc = (st["ax"], st["ay"], st["az"])
+    ref = nb.Sim(nb.Config(method=nb.DIRECT_MIXED, G=1.0, softening=EPS), capacity=n,
+                 stream=stream.cuda_stream)
+    ref.load(st["x"], st["y"], st["z"], st["vx"], st["vy"], st["vz"], st["m"])
+    ref.compute_forces()
+    ra = ref.accelerations()
+    ref.close()
+    d = np.sqrt(sum((u - v) ** 2 for u, v in zip(bh_acc, ra)))
+    r = np.sqrt(sum(v * v for v in ra))
+    rel = d / np.maximum(r, 1e-300)
+    out["force_error_vs_direct"] = {"mean_rel": float(rel.mean()), "max_rel": float(rel.max()),
+                                    "p99_rel": float(np.quantile(rel, 0.99))}
+    sim.close()
+    return out
 
 
 # ---------------------------------------------------------------- our arm
@@ -275,12 +359,8 @@ def run_ours(a, rank, world, local_rank):
     if clk.get("sm_mhz"):
         roofline["frac_at_measured_clock"] = achieved / fp32_roofline_gint(
             props.multi_processor_count, clk["sm_mhz"])
-    tp = os.path.join(REPO, "profiles", "direct_mixed_n65536_traffic.json")
-    if os.path.exists(tp) and n == N_BODIES:
-        try:
-            roofline["traffic"] = json.load(open(tp)).get("dram_bytes_per_launch")
-        except ValueError:
-            pass
+    roofline["traffic"] = profiled_traffic("direct_mixed_n65536.md") if n == N_BODIES else None
+    roofline["algorithmic_bytes"] = 32 * n  # hi + lo mirror of every body, read once
 
     extras = {}
     if not a.skip_extras and rank == 0:
@@ -316,6 +396,9 @@ def run_ours(a, rank, world, local_rank):
                                                                      np.sqrt(np.mean(r * r)))}
         extras["fp64_direct"] = {"gint_s": fp64_rate, "kernel": "direct_fp64_kernel",
                                  "mixed_speedup": achieved / fp64_rate}
+
+    if not a.skip_extras and rank == 0 and a.bh_steps > 0:
+        extras["barnes_hut"] = run_bh(a, nb, torch, dev, stream, flush, np)
 
     # e2e: one force evaluation through the C ABI with pinned host buffers
     e2e = None

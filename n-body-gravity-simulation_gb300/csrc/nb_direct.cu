@@ -28,6 +28,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 
@@ -303,24 +306,147 @@ constexpr int kMixIpt = 4;
 constexpr int kF64Block = 128;
 constexpr int kF64Ipt = 2;
 
+// Tile shapes of the mixed kernel the autotuner chooses from: threads per CTA
+// x i-bodies per thread.  More i-bodies per thread amortise the two
+// broadcast shared-memory loads of a j-body and add independent work per
+// warp; fewer keep more warps resident.
+struct MixShape {
+    int block, ipt;
+};
+constexpr MixShape kMixShapes[] = {{256, 4}, {128, 8}, {128, 4}, {256, 2}, {64, 8}};
+constexpr int kNumMixShapes = sizeof(kMixShapes) / sizeof(kMixShapes[0]);
+
+template <int B, int I>
+int mix_slots()
+{
+    static int slots = 0;
+    if (!slots) slots = resident_ctas<B, I>((const void *)direct_mixed_kernel<B, I, false>);
+    return slots;
+}
+
+int mix_slots_for(int block, int ipt)
+{
+    if (block == 256 && ipt == 4) return mix_slots<256, 4>();
+    if (block == 128 && ipt == 8) return mix_slots<128, 8>();
+    if (block == 128 && ipt == 4) return mix_slots<128, 4>();
+    if (block == 256 && ipt == 2) return mix_slots<256, 2>();
+    if (block == 64 && ipt == 8) return mix_slots<64, 8>();
+    return 0;
+}
+
+template <int B, int I>
+void launch_mixed_shape(dim3 grid, cudaStream_t st, const float4 *hi, const float4 *lo, int n,
+                        double eps2, int seg_len, float *psum, float *pcomp)
+{
+    if (eps2 > 0.0)
+        direct_mixed_kernel<B, I, false>
+            <<<grid, B, 0, st>>>(hi, lo, n, (float)eps2, seg_len, psum, pcomp);
+    else
+        direct_mixed_kernel<B, I, true><<<grid, B, 0, st>>>(hi, lo, n, 0.0f, seg_len, psum, pcomp);
+}
+
+// Launches the all-pairs kernel of plan p (partials psum/pcomp sized for
+// p.segments); returns false for a shape that is not compiled in.
+bool launch_mixed(const DirectPlan &p, cudaStream_t st, const float4 *hi, const float4 *lo,
+                  int n, double eps2, float *psum, float *pcomp)
+{
+    const int per_cta = p.block * p.ipt;
+    dim3 grid((n + per_cta - 1) / per_cta, p.segments);
+    const int seg_len = p.seg_tiles * p.block;
+    if (p.block == 256 && p.ipt == 4)
+        launch_mixed_shape<256, 4>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
+    else if (p.block == 128 && p.ipt == 8)
+        launch_mixed_shape<128, 8>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
+    else if (p.block == 128 && p.ipt == 4)
+        launch_mixed_shape<128, 4>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
+    else if (p.block == 256 && p.ipt == 2)
+        launch_mixed_shape<256, 2>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
+    else if (p.block == 64 && p.ipt == 8)
+        launch_mixed_shape<64, 8>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
+    else
+        return false;
+    return true;
+}
+
+DirectPlan plan_for_shape(int n, int block, int ipt)
+{
+    DirectPlan p;
+    p.block = block;
+    p.ipt = ipt;
+    const int per_cta = block * ipt;
+    const int iblocks = (n + per_cta - 1) / per_cta;
+    const int tiles = (n + block - 1) / block;
+    p.segments = pick_segments(iblocks, tiles, mix_slots_for(block, ipt));
+    p.seg_tiles = (tiles + p.segments - 1) / p.segments;
+    p.segments = (tiles + p.seg_tiles - 1) / p.seg_tiles;
+    return p;
+}
+
+// Autotuned plans by body count (the tuner times every shape on the caller's
+// own bodies at the first evaluation of each N; NB_AUTOTUNE=0 disables it).
+std::mutex g_tune_mutex;
+std::map<int, DirectPlan> g_tuned;
+
+bool autotune_enabled()
+{
+    static const bool on = [] {
+        const char *e = std::getenv("NB_AUTOTUNE");
+        return !(e && std::strcmp(e, "0") == 0);
+    }();
+    return on;
+}
+
 } // namespace
 
 DirectPlan direct_mixed_plan(int n)
 {
-    DirectPlan p;
-    p.block = kMixBlock;
-    p.ipt = kMixIpt;
-    const int per_cta = p.block * p.ipt;
-    const int iblocks = (n + per_cta - 1) / per_cta;
-    const int tiles = (n + p.block - 1) / p.block;
-    static int slots = 0;
-    if (!slots)
-        slots = resident_ctas<kMixBlock, kMixIpt>(
-            (const void *)direct_mixed_kernel<kMixBlock, kMixIpt, false>);
-    p.segments = pick_segments(iblocks, tiles, slots);
-    p.seg_tiles = (tiles + p.segments - 1) / p.segments;
-    p.segments = (tiles + p.seg_tiles - 1) / p.seg_tiles;
-    return p;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tuned.find(n);
+        if (it != g_tuned.end()) return it->second;
+    }
+    return plan_for_shape(n, kMixBlock, kMixIpt);
+}
+
+// Times every tile shape on the given bodies (two launches each after one
+// warm-up, CUDA events on `st`) and records the fastest for this n.
+static nb_status autotune_mixed(const float4 *hi, const float4 *lo, int n, double eps2,
+                                DevBuf &partials, cudaStream_t st, DirectPlan *best)
+{
+    DirectPlan plans[kNumMixShapes];
+    size_t need = 0;
+    for (int k = 0; k < kNumMixShapes; ++k) {
+        plans[k] = plan_for_shape(n, kMixShapes[k].block, kMixShapes[k].ipt);
+        need = std::max(need, sizeof(float) * 6 * (size_t)n * plans[k].segments);
+    }
+    NB_TRY(partials.reserve(need));
+    cudaEvent_t e0, e1;
+    NB_CUDA_TRY(cudaEventCreate(&e0));
+    NB_CUDA_TRY(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    *best = plans[0];
+    for (int k = 0; k < kNumMixShapes; ++k) {
+        float *psum = partials.as<float>();
+        float *pcomp = psum + 3 * (size_t)n * plans[k].segments;
+        launch_mixed(plans[k], st, hi, lo, n, eps2, psum, pcomp);
+        NB_LAUNCH_CHECK();
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < 2; ++r) launch_mixed(plans[k], st, hi, lo, n, eps2, psum, pcomp);
+        cudaEventRecord(e1, st);
+        NB_LAUNCH_CHECK();
+        NB_CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_ms) {
+            best_ms = ms;
+            *best = plans[k];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tuned[n] = *best;
+    return NB_OK;
 }
 
 nb_status split_positions(const double *x, const double *y, const double *z, const double *m,
@@ -337,22 +463,26 @@ nb_status direct_mixed(const float4 *hi, const float4 *lo, int n, double G, doub
                        const KernelTimer *timer, const DirectPlan *plan_override)
 {
     if (n <= 0) return NB_OK;
-    const DirectPlan p = plan_override ? *plan_override : direct_mixed_plan(n);
-    if (p.block != kMixBlock || p.ipt != kMixIpt)
-        return fail(NB_ERR_UNSUPPORTED, "direct_mixed: unsupported tile shape");
+    DirectPlan p;
+    if (plan_override) {
+        p = *plan_override;
+    } else {
+        bool tuned;
+        {
+            std::lock_guard<std::mutex> lock(g_tune_mutex);
+            tuned = g_tuned.count(n) != 0;
+        }
+        if (!tuned && autotune_enabled() && n >= 4096)
+            NB_TRY(autotune_mixed(hi, lo, n, eps2, partials, st, &p));
+        else
+            p = direct_mixed_plan(n);
+    }
     NB_TRY(partials.reserve(sizeof(float) * 6 * (size_t)n * p.segments));
     float *psum = partials.as<float>();
     float *pcomp = psum + 3 * (size_t)n * p.segments;
-    const int per_cta = p.block * p.ipt;
-    dim3 grid((n + per_cta - 1) / per_cta, p.segments);
-    const int seg_len = p.seg_tiles * p.block;
     if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
-    if (eps2 > 0.0)
-        direct_mixed_kernel<kMixBlock, kMixIpt, false>
-            <<<grid, kMixBlock, 0, st>>>(hi, lo, n, (float)eps2, seg_len, psum, pcomp);
-    else
-        direct_mixed_kernel<kMixBlock, kMixIpt, true>
-            <<<grid, kMixBlock, 0, st>>>(hi, lo, n, 0.0f, seg_len, psum, pcomp);
+    if (!launch_mixed(p, st, hi, lo, n, eps2, psum, pcomp))
+        return fail(NB_ERR_UNSUPPORTED, "direct_mixed: unsupported tile shape");
     NB_LAUNCH_CHECK();
     if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
     combine_mixed_kernel<<<(n + 255) / 256, 256, 0, st>>>(psum, pcomp, n, p.segments, G, ax, ay,
@@ -491,15 +621,8 @@ extern "C" nb_status nb_direct_mixed_forces_noalloc(size_t n, const double *x, c
     split_kernel<<<(ni + 255) / 256, 256, 0, st>>>(x, y, z, m, ni, hi, lo);
     NB_LAUNCH_CHECK();
     const double eps2 = softening * softening;
-    const int per_cta = p.block * p.ipt;
-    dim3 grid((ni + per_cta - 1) / per_cta, p.segments);
-    const int seg_len = p.seg_tiles * p.block;
-    if (eps2 > 0.0)
-        direct_mixed_kernel<kMixBlock, kMixIpt, false>
-            <<<grid, kMixBlock, 0, st>>>(hi, lo, ni, (float)eps2, seg_len, psum, pcomp);
-    else
-        direct_mixed_kernel<kMixBlock, kMixIpt, true>
-            <<<grid, kMixBlock, 0, st>>>(hi, lo, ni, 0.0f, seg_len, psum, pcomp);
+    if (!launch_mixed(p, st, hi, lo, ni, eps2, psum, pcomp))
+        return fail(NB_ERR_UNSUPPORTED, "nb_direct_mixed_forces_noalloc: tile shape");
     NB_LAUNCH_CHECK();
     combine_mixed_kernel<<<(ni + 255) / 256, 256, 0, st>>>(psum, pcomp, ni, p.segments, G, ax,
                                                           ay, az);
