@@ -200,6 +200,50 @@ nb_status nb_bh_read_order(nb_sim *sim, uint64_t *sorted_codes, uint32_t *order)
 nb_status nb_bh_read_nodes(nb_sim *sim, int max_nodes, int *depth, uint64_t *prefix,
                            int *first, int *count, int *is_leaf, int *skip, float *com_mass);
 
+/* ---- batched ensemble ------------------------------------------------------ */
+
+/* No counterpart in the reference (one system per process there).  Many
+ * independent systems of uneven N, concatenated in system order, advanced
+ * together: mixed-precision direct forces of all systems in one persistent
+ * launch over a per-system work queue, per-body updates over the
+ * concatenation, the step loop captured in a CUDA graph and replayed.
+ * i-bodies per lane are autotuned per N bucket on the loaded systems at the
+ * first evaluation (or by nb_ensemble_tune).  A system's result does not
+ * depend on the other systems of the ensemble. */
+typedef struct nb_ensemble nb_ensemble;
+
+typedef struct nb_ensemble_info_t {
+    int num_systems;
+    int64_t total_bodies;
+    double interactions_per_eval;   /* sum over systems of n (n - 1) */
+    int work_items;
+    int ipt_by_bucket[32];          /* i-bodies per lane for n in [2^b, 2^(b+1)) */
+    uint64_t graph_launches;        /* replays of the captured step loop so far */
+    int graph_steps;                /* steps per replay */
+    uint64_t force_launches;        /* timed force launches while profiling */
+    double force_kernel_ms;         /* their summed device time */
+} nb_ensemble_info_t;
+
+/* cfg->method must be NB_DIRECT_MIXED.  stream NULL: the ensemble makes its
+ * own (graph capture needs a stream other than the legacy default one). */
+nb_status nb_ensemble_create(const nb_config *cfg, int num_systems, const int *sizes,
+                             void *stream, nb_ensemble **out);
+nb_status nb_ensemble_destroy(nb_ensemble *e);
+/* Host arrays of sum(sizes) bodies, systems concatenated in order. */
+nb_status nb_ensemble_load(nb_ensemble *e, const double *x, const double *y, const double *z,
+                           const double *vx, const double *vy, const double *vz,
+                           const double *m);
+nb_status nb_ensemble_read_state(nb_ensemble *e, double *x, double *y, double *z, double *vx,
+                                 double *vy, double *vz, double *ax, double *ay, double *az,
+                                 double *m);
+nb_status nb_ensemble_compute_forces(nb_ensemble *e);
+nb_status nb_ensemble_step(nb_ensemble *e, int integrator, double dt, int nsteps);
+nb_status nb_ensemble_tune(nb_ensemble *e, int *ipt_by_bucket /* 32 entries or NULL */);
+nb_status nb_ensemble_synchronize(nb_ensemble *e);
+nb_status nb_ensemble_info(nb_ensemble *e, nb_ensemble_info_t *info);
+/* Times every force launch with events (and runs steps without the graph). */
+nb_status nb_ensemble_profile(nb_ensemble *e, int enable);
+
 /* ---- host-side input generators (no GPU needed) ------------------------- */
 
 /* Equal-mass Plummer sphere (total mass M, scale radius a, G), positions and

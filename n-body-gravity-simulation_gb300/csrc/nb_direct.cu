@@ -25,6 +25,7 @@
 // all 152 SMs busy at small N (the reference runs 4 CTAs at N = 1024) and the
 // segment count is chosen to fill whole waves.
 #include "nb_internal.h"
+#include "nb_pair.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -36,27 +37,6 @@
 
 namespace nb {
 namespace {
-
-__device__ __forceinline__ float rsqrt_mufu(float x)
-{
-    float r;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
-// Padding body for the tail of the last tile: massless and far away, so that
-// its pair term is exactly zero (s = 0 * finite) for every i-body.
-__device__ __forceinline__ float4 far_body() { return make_float4(1.0e18f, 1.0e18f, 1.0e18f, 0.0f); }
-
-// Kahan-compensated add of t into (s, c).  Plain FP32 adds: no product, so
-// nothing can be contracted into an FMA.
-__device__ __forceinline__ void kahan_add(float &s, float &c, float t)
-{
-    float y = t - c;
-    float u = s + y;
-    c = (u - s) - y;
-    s = u;
-}
 
 template <int BLOCK, int IPT, bool ZERO_SOFT>
 __global__ void __launch_bounds__(BLOCK)
@@ -115,24 +95,9 @@ direct_mixed_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo
             const float4 H = sh_hi[jj];
             const float4 L = sh_lo[jj];
 #pragma unroll
-            for (int k = 0; k < IPT; ++k) {
-                const float dx = (H.x - xh[k]) + (L.x - xl[k]);
-                const float dy = (H.y - yh[k]) + (L.y - yl[k]);
-                const float dz = (H.z - zh[k]) + (L.z - zl[k]);
-                const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-                float inv = rsqrt_mufu(r2);
-                if (ZERO_SOFT) inv = (r2 > 0.f) ? inv : 0.f;  // the j == i term
-                const float inv2 = inv * inv;
-                // MUFU rsqrt is good to ~1.3e-7; y^3 with y = y0 (1 + d) is
-                // y0^3 (1 - 3d) to first order and r2 y0^2 = 1 + 2d, so
-                // y^3 ~= y0^3 (2.5 - 1.5 r2 y0^2): one Newton step folded
-                // into the cube (3 FP32 ops) leaves an O(d^2) error.
-                const float corr = fmaf(-1.5f, r2 * inv2, 2.5f);
-                const float s = ((H.w * inv) * inv2) * corr;
-                ax[k] = fmaf(dx, s, ax[k]);
-                ay[k] = fmaf(dy, s, ay[k]);
-                az[k] = fmaf(dz, s, az[k]);
-            }
+            for (int k = 0; k < IPT; ++k)
+                pair_term<ZERO_SOFT>(H, L, xh[k], yh[k], zh[k], xl[k], yl[k], zl[k], eps2,
+                                     ax[k], ay[k], az[k]);
         }
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {

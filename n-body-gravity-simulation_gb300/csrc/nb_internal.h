@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -114,10 +115,45 @@ nb_status rk4_combine(int n, double dt, double *x, double *y, double *z, double 
                       const double *az, const double *k2, const double *k3, const double *k4,
                       cudaStream_t st);
 
+// One integrator step over the ten FP64 planes f (x y z vx vy vz ax ay az m)
+// of n bodies; `force` evaluates accelerations of given positions.
+struct StepBuffers {
+    double *old_acc = nullptr;  // 3 planes (velocity Verlet)
+    double *rk4 = nullptr;      // 27 planes (RK4 stages K2, K3, K4: x v a each)
+    size_t ps = 0;              // plane stride in doubles
+};
+using ForceFn = std::function<nb_status(const double *, const double *, const double *,
+                                        double *, double *, double *)>;
+nb_status integrate_step(int integ, int n, double dt, double *const f[10], StepBuffers &b,
+                         bool &forces_valid, const ForceFn &force, cudaStream_t st);
+
 // ---------------------------------------------------------------- diagnostics
 nb_status diagnostics(const double *x, const double *y, const double *z, const double *vx,
                       const double *vy, const double *vz, const double *m, int n, double G,
                       double eps2, DevBuf &scratch, cudaStream_t st, nb_diag *out);
+
+// ---------------------------------------------------------------- batches
+// A system of a batch: bodies [first, first + n) of the batch's pool, summed
+// with ipt i-bodies per lane.
+struct SysDesc {
+    int first;
+    int n;
+    int ipt;
+    int pad;
+};
+// One queue item: i-bodies [i0, i0 + 32 * ipt) of system `sys`.
+struct WorkItem {
+    int sys;
+    int i0;
+};
+int bucket_of(int n);  // floor(log2(n))
+// Items of every system, largest cost first.
+void build_work_items(const std::vector<SysDesc> &sys, std::vector<WorkItem> &items);
+// Mixed-precision forces of all systems of the queue (persistent kernel).
+nb_status batch_forces(const float4 *hi, const float4 *lo, const SysDesc *d_sys,
+                       const WorkItem *d_items, int num_items, int *d_counter, double G,
+                       double eps2, double *ax, double *ay, double *az, cudaStream_t st,
+                       const KernelTimer *timer = nullptr);
 
 // ---------------------------------------------------------------- Barnes-Hut
 struct BHTree;  // opaque, defined in nb_bh.cu

@@ -42,6 +42,9 @@ EXPORTS = [
     "nb_gen_plummer", "nb_gen_disk_bulge", "nb_status_string", "nb_last_error", "nb_version",
     "nb_profile_enable", "nb_profile_read", "nb_kernel_launch_count",
     "nb_direct_mixed_forces_noalloc",
+    "nb_ensemble_create", "nb_ensemble_destroy", "nb_ensemble_load", "nb_ensemble_read_state",
+    "nb_ensemble_compute_forces", "nb_ensemble_step", "nb_ensemble_tune",
+    "nb_ensemble_synchronize", "nb_ensemble_info", "nb_ensemble_profile",
 ]
 _NON_STATUS = {"nb_status_string", "nb_last_error", "nb_version", "nb_kernel_launch_count"}
 
@@ -73,6 +76,14 @@ class _BHInfo(C.Structure):
 
 class _Profile(C.Structure):
     _fields_ = [("kernel_launches", C.c_uint64), ("force_launches", C.c_uint64),
+                ("force_kernel_ms", C.c_double)]
+
+
+class _EnsembleInfo(C.Structure):
+    _fields_ = [("num_systems", C.c_int), ("total_bodies", C.c_int64),
+                ("interactions_per_eval", C.c_double), ("work_items", C.c_int),
+                ("ipt_by_bucket", C.c_int * 32), ("graph_launches", C.c_uint64),
+                ("graph_steps", C.c_int), ("force_launches", C.c_uint64),
                 ("force_kernel_ms", C.c_double)]
 
 
@@ -143,6 +154,16 @@ def lib():
     L.nb_kernel_launch_count.restype = C.c_uint64
     L.nb_direct_mixed_forces_noalloc.argtypes = ([sz] + [vp] * 4 + [C.c_double] * 2 +
                                                  [vp] * 3 + [vp])
+    L.nb_ensemble_create.argtypes = [C.POINTER(_Config), C.c_int, vp, vp, C.POINTER(vp)]
+    L.nb_ensemble_destroy.argtypes = [vp]
+    L.nb_ensemble_load.argtypes = [vp] + [vp] * 7
+    L.nb_ensemble_read_state.argtypes = [vp] + [vp] * 10
+    L.nb_ensemble_compute_forces.argtypes = [vp]
+    L.nb_ensemble_step.argtypes = [vp, C.c_int, C.c_double, C.c_int]
+    L.nb_ensemble_tune.argtypes = [vp, vp]
+    L.nb_ensemble_synchronize.argtypes = [vp]
+    L.nb_ensemble_info.argtypes = [vp, C.POINTER(_EnsembleInfo)]
+    L.nb_ensemble_profile.argtypes = [vp, C.c_int]
     for name in EXPORTS:
         f = getattr(L, name)
         if name not in _NON_STATUS:
@@ -337,6 +358,103 @@ class Sim:
                                       _ptr(a["skip"]), _ptr(a["com_mass"])),
                "nb_bh_read_nodes")
         return a
+
+
+class Ensemble:
+    """Many independent systems advanced together (nb_ensemble)."""
+
+    def __init__(self, config: Config, sizes, stream: int | None = None):
+        self._h = C.c_void_p()
+        self.sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes, dtype=np.int64)])
+        cfg = config._c()
+        _check(lib().nb_ensemble_create(C.byref(cfg), len(self.sizes), _ptr(self.sizes),
+                                        C.c_void_p(stream or 0), C.byref(self._h)),
+               "nb_ensemble_create")
+
+    def close(self):
+        if self._h:
+            lib().nb_ensemble_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def total(self) -> int:
+        return int(self.offsets[-1])
+
+    def load(self, x, y, z, vx, vy, vz, m):
+        arrs = [_f64(a) for a in (x, y, z, vx, vy, vz, m)]
+        if any(len(a) != self.total for a in arrs):
+            raise ValueError("arrays must hold sum(sizes) bodies")
+        _check(lib().nb_ensemble_load(self._h, *map(_ptr, arrs)), "nb_ensemble_load")
+
+    def read_state(self):
+        out = [np.empty(self.total) for _ in range(10)]
+        _check(lib().nb_ensemble_read_state(self._h, *map(_ptr, out)), "nb_ensemble_read_state")
+        keys = ["x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "m"]
+        return dict(zip(keys, out))
+
+    def system(self, state: dict, s: int) -> dict:
+        a, b = self.offsets[s], self.offsets[s + 1]
+        return {k: v[a:b] for k, v in state.items()}
+
+    def compute_forces(self):
+        _check(lib().nb_ensemble_compute_forces(self._h), "nb_ensemble_compute_forces")
+
+    def step(self, integrator: int, dt: float, nsteps: int = 1):
+        _check(lib().nb_ensemble_step(self._h, integrator, dt, nsteps), "nb_ensemble_step")
+
+    def tune(self):
+        out = np.zeros(32, np.int32)
+        _check(lib().nb_ensemble_tune(self._h, _ptr(out)), "nb_ensemble_tune")
+        return out
+
+    def synchronize(self):
+        _check(lib().nb_ensemble_synchronize(self._h), "nb_ensemble_synchronize")
+
+    def profile(self, enable: bool = True):
+        _check(lib().nb_ensemble_profile(self._h, int(enable)), "nb_ensemble_profile")
+
+    def info(self) -> dict:
+        i = _EnsembleInfo()
+        _check(lib().nb_ensemble_info(self._h, C.byref(i)), "nb_ensemble_info")
+        return dict(num_systems=i.num_systems, total_bodies=i.total_bodies,
+                    interactions_per_eval=i.interactions_per_eval, work_items=i.work_items,
+                    ipt_by_bucket=list(i.ipt_by_bucket), graph_launches=i.graph_launches,
+                    graph_steps=i.graph_steps, force_launches=i.force_launches,
+                    force_kernel_ms=i.force_kernel_ms)
+
+
+def ensemble_sizes(num_systems: int, lo: int, hi: int, seed: int):
+    """N per system, log-uniform in [lo, hi] (SplitMix64 keyed by seed and
+    system index, as the generators)."""
+    out = np.empty(num_systems, np.int64)
+    for s in range(num_systems):
+        z = (seed * 0xD1B54A32D192ED03 ^ (s + 1) * 0x9E3779B97F4A7C15) & (2**64 - 1)
+        z = (z + 0x9E3779B97F4A7C15) & (2**64 - 1)
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & (2**64 - 1)
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & (2**64 - 1)
+        z ^= z >> 31
+        u = ((z >> 11) + 0.5) / 2.0**53
+        out[s] = int(np.floor(np.exp(np.log(lo) + u * (np.log(hi + 1) - np.log(lo)))))
+    return np.clip(out, lo, hi)
+
+
+def plummer_ensemble(sizes, seed: int = 0):
+    """Concatenated Plummer spheres (G = M = a = 1), system s seeded with seed + s."""
+    parts = [plummer(int(n), seed=seed + s) for s, n in enumerate(sizes)]
+    return tuple(np.concatenate([p[k] for p in parts]) for k in range(7))
 
 
 def _bh_info_dict(info) -> dict:
