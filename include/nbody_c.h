@@ -244,6 +244,58 @@ nb_status nb_ensemble_info(nb_ensemble *e, nb_ensemble_info_t *info);
 /* Times every force launch with events (and runs steps without the graph). */
 nb_status nb_ensemble_profile(nb_ensemble *e, int enable);
 
+/* ---- serving loop ------------------------------------------------------------ */
+
+/* No counterpart in the reference.  A continuous-batching server for
+ * simulation jobs: each nb_server_tick admits queued jobs while their device
+ * memory fits the HBM budget, advances every running job by one leapfrog
+ * step (direct jobs together in one batched launch over a resident body
+ * pool, Barnes-Hut jobs on their own streams, overlapping), and retires jobs
+ * that reached their step count.  A job's result does not depend on the other
+ * jobs it ran with. */
+typedef struct nb_server nb_server;
+
+typedef struct nb_server_config {
+    double G;
+    double softening;
+    double theta;            /* Barnes-Hut jobs */
+    int leaf_capacity;       /* Barnes-Hut jobs */
+    int direct_max_n;        /* jobs with n < direct_max_n use the direct sum */
+    double dt;               /* leapfrog step */
+    size_t hbm_budget_bytes; /* device memory for job state, pool included */
+    size_t pool_bodies;      /* capacity of the direct-job body pool */
+} nb_server_config;
+
+typedef struct nb_server_stats {
+    uint64_t jobs_submitted, jobs_finished;
+    int jobs_running, jobs_queued;
+    uint64_t steps_done, ticks;
+    double interactions;     /* pair (direct) + body-node and body-body (tree) terms */
+    double busy_ms;          /* sum of tick device times */
+    double step_ms_p50, step_ms_p99;   /* per job step: tick start -> step complete */
+    double queue_ms_p50, queue_ms_p99; /* submission -> admission (wall clock) */
+    int max_running;
+    size_t peak_device_bytes;
+} nb_server_stats;
+
+/* G 1, softening 1e-3, theta 0.6, leaf 8, direct below 16384 bodies, dt 1e-3,
+ * 16 GiB budget, 4 Mi-body pool. */
+nb_status nb_server_config_default(nb_server_config *cfg);
+nb_status nb_server_create(const nb_server_config *cfg, nb_server **out);
+nb_status nb_server_destroy(nb_server *s);
+/* Copies the host arrays; the job waits in the queue until admitted. */
+nb_status nb_server_submit(nb_server *s, size_t n, const double *x, const double *y,
+                           const double *z, const double *vx, const double *vy,
+                           const double *vz, const double *m, int steps, int64_t *job_id);
+nb_status nb_server_tick(nb_server *s, int *running, int *queued);
+/* State of a finished job (NB_ERR_NOT_LOADED until it finished). */
+nb_status nb_server_result(nb_server *s, int64_t job_id, double *x, double *y, double *z,
+                           double *vx, double *vy, double *vz, double *ax, double *ay,
+                           double *az, double *m);
+/* Drops a finished job's stored result. */
+nb_status nb_server_release(nb_server *s, int64_t job_id);
+nb_status nb_server_get_stats(nb_server *s, nb_server_stats *out);
+
 /* ---- host-side input generators (no GPU needed) ------------------------- */
 
 /* Equal-mass Plummer sphere (total mass M, scale radius a, G), positions and

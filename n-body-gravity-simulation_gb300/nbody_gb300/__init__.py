@@ -45,6 +45,8 @@ EXPORTS = [
     "nb_ensemble_create", "nb_ensemble_destroy", "nb_ensemble_load", "nb_ensemble_read_state",
     "nb_ensemble_compute_forces", "nb_ensemble_step", "nb_ensemble_tune",
     "nb_ensemble_synchronize", "nb_ensemble_info", "nb_ensemble_profile",
+    "nb_server_config_default", "nb_server_create", "nb_server_destroy", "nb_server_submit",
+    "nb_server_tick", "nb_server_result", "nb_server_release", "nb_server_get_stats",
 ]
 _NON_STATUS = {"nb_status_string", "nb_last_error", "nb_version", "nb_kernel_launch_count"}
 
@@ -85,6 +87,22 @@ class _EnsembleInfo(C.Structure):
                 ("ipt_by_bucket", C.c_int * 32), ("graph_launches", C.c_uint64),
                 ("graph_steps", C.c_int), ("force_launches", C.c_uint64),
                 ("force_kernel_ms", C.c_double)]
+
+
+class _ServerConfig(C.Structure):
+    _fields_ = [("G", C.c_double), ("softening", C.c_double), ("theta", C.c_double),
+                ("leaf_capacity", C.c_int), ("direct_max_n", C.c_int), ("dt", C.c_double),
+                ("hbm_budget_bytes", C.c_size_t), ("pool_bodies", C.c_size_t)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [("jobs_submitted", C.c_uint64), ("jobs_finished", C.c_uint64),
+                ("jobs_running", C.c_int), ("jobs_queued", C.c_int),
+                ("steps_done", C.c_uint64), ("ticks", C.c_uint64),
+                ("interactions", C.c_double), ("busy_ms", C.c_double),
+                ("step_ms_p50", C.c_double), ("step_ms_p99", C.c_double),
+                ("queue_ms_p50", C.c_double), ("queue_ms_p99", C.c_double),
+                ("max_running", C.c_int), ("peak_device_bytes", C.c_size_t)]
 
 
 def kernel_launch_count() -> int:
@@ -164,6 +182,14 @@ def lib():
     L.nb_ensemble_synchronize.argtypes = [vp]
     L.nb_ensemble_info.argtypes = [vp, C.POINTER(_EnsembleInfo)]
     L.nb_ensemble_profile.argtypes = [vp, C.c_int]
+    L.nb_server_config_default.argtypes = [C.POINTER(_ServerConfig)]
+    L.nb_server_create.argtypes = [C.POINTER(_ServerConfig), C.POINTER(vp)]
+    L.nb_server_destroy.argtypes = [vp]
+    L.nb_server_submit.argtypes = [vp, sz] + [vp] * 7 + [C.c_int, C.POINTER(C.c_int64)]
+    L.nb_server_tick.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.nb_server_result.argtypes = [vp, C.c_int64] + [vp] * 10
+    L.nb_server_release.argtypes = [vp, C.c_int64]
+    L.nb_server_get_stats.argtypes = [vp, C.POINTER(_ServerStats)]
     for name in EXPORTS:
         f = getattr(L, name)
         if name not in _NON_STATUS:
@@ -434,6 +460,70 @@ class Ensemble:
                     ipt_by_bucket=list(i.ipt_by_bucket), graph_launches=i.graph_launches,
                     graph_steps=i.graph_steps, force_launches=i.force_launches,
                     force_kernel_ms=i.force_kernel_ms)
+
+
+class Server:
+    """Continuous-batching job server (nb_server)."""
+
+    def __init__(self, **overrides):
+        c = _ServerConfig()
+        _check(lib().nb_server_config_default(C.byref(c)), "nb_server_config_default")
+        for k, v in overrides.items():
+            setattr(c, k, v)
+        self._h = C.c_void_p()
+        _check(lib().nb_server_create(C.byref(c), C.byref(self._h)), "nb_server_create")
+        self.sizes = {}
+
+    def close(self):
+        if self._h:
+            lib().nb_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, state, steps: int) -> int:
+        arrs = [_f64(a) for a in state]
+        jid = C.c_int64()
+        _check(lib().nb_server_submit(self._h, len(arrs[0]), *map(_ptr, arrs), steps,
+                                      C.byref(jid)), "nb_server_submit")
+        self.sizes[jid.value] = len(arrs[0])
+        return jid.value
+
+    def tick(self):
+        r, q = C.c_int(), C.c_int()
+        _check(lib().nb_server_tick(self._h, C.byref(r), C.byref(q)), "nb_server_tick")
+        return r.value, q.value
+
+    def result(self, job_id: int):
+        n = self.sizes[job_id]
+        out = [np.empty(n) for _ in range(10)]
+        _check(lib().nb_server_result(self._h, job_id, *map(_ptr, out)), "nb_server_result")
+        return dict(zip(["x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "m"], out))
+
+    def release(self, job_id: int):
+        _check(lib().nb_server_release(self._h, job_id), "nb_server_release")
+
+    def stats(self) -> dict:
+        s = _ServerStats()
+        _check(lib().nb_server_get_stats(self._h, C.byref(s)), "nb_server_get_stats")
+        return {k: getattr(s, k) for k, _ in _ServerStats._fields_}
+
+    def run_until_idle(self, max_ticks: int = 10**7):
+        for _ in range(max_ticks):
+            r, q = self.tick()
+            if r == 0 and q == 0:
+                return
+        raise RuntimeError("server did not drain")
 
 
 def ensemble_sizes(num_systems: int, lo: int, hi: int, seed: int):
