@@ -58,6 +58,12 @@ def parse():
     ap.add_argument("--bh-steps", type=int, default=20,
                     help="leapfrog steps of the Barnes-Hut N=2^20 extra (0 skips it)")
     ap.add_argument("--bh-n", type=int, default=1 << 20)
+    ap.add_argument("--ens-steps", type=int, default=25,
+                    help="RK4 steps of the 4096-system ensemble extra (0 skips it)")
+    ap.add_argument("--ens-systems", type=int, default=4096)
+    ap.add_argument("--serve-seconds", type=float, default=1.0,
+                    help="seconds of Poisson arrivals for the serving extra (0 skips it)")
+    ap.add_argument("--serve-rate", type=float, default=200.0)
     return ap.parse_args()
 
 
@@ -284,6 +290,93 @@ def run_bh(a, nb, torch, dev, stream, flush, np):
     return out
 
 
+# ---------------------------------------------------------------- ensemble
+def run_ensemble(a, nb, torch, stream):
+    """The batched-ensemble configuration: 4096 Plummer spheres (system s
+    seeded with s), N log-uniform in [32, 4096], mixed direct forces, RK4
+    dt = 1e-3; a.ens_steps steps replayed from the captured CUDA graph, timed
+    with events around the whole loop (4 force evaluations per step)."""
+    sizes = nb.ensemble_sizes(a.ens_systems, 32, 4096, SEED)
+    state = nb.plummer_ensemble(sizes, seed=SEED)
+    # graph capture needs a stream of its own (not the legacy default stream)
+    stream = torch.cuda.Stream()
+    e = nb.Ensemble(nb.Config(method=nb.DIRECT_MIXED, G=1.0, softening=EPS), sizes,
+                    stream=stream.cuda_stream)
+    e.load(*state)
+    e.step(nb.RK4, 1e-3, 2 * 25)  # tunes, captures the graph, warms up
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    e.step(nb.RK4, 1e-3, a.ens_steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / a.ens_steps
+    info = e.info()
+    # the force kernel alone, timed per launch (steps without the graph)
+    e.profile(True)
+    e.step(nb.RK4, 1e-3, 2)
+    pinfo = e.info()
+    e.close()
+    inter = info["interactions_per_eval"]
+    kernel_ms = pinfo["force_kernel_ms"] / max(1, pinfo["force_launches"])
+    return {"workload": f"{a.ens_systems}_plummer_systems_n32_4096_rk4",
+            "systems": a.ens_systems, "bodies": int(sizes.sum()),
+            "interactions_per_eval": inter, "steps": a.ens_steps, "ms_per_step": ms,
+            "ginteractions_s": 4 * inter / (ms / 1e3) / 1e9,
+            "force_kernel_ms": kernel_ms,
+            "force_kernel_ginteractions_s": inter / (kernel_ms / 1e3) / 1e9,
+            "work_items": info["work_items"], "graph_steps_per_replay": info["graph_steps"],
+            "ipt_by_bucket": {str(b): info["ipt_by_bucket"][b] for b in range(5, 13)},
+            "timing": "CUDA events around the graph-replayed step loop"}
+
+
+# ---------------------------------------------------------------- serving
+def run_serving(a, nb, np):
+    """The serving configuration, shortened: Poisson arrivals at a.serve_rate
+    jobs/s for a.serve_seconds of wall time, N log-uniform in [1024, 262144],
+    Plummer or disk+bulge (alternating), 100 leapfrog steps each, direct below
+    16384 bodies and Barnes-Hut theta 0.6 above; the server admits by HBM
+    budget and ticks until drained."""
+    rng = np.random.default_rng(SEED)
+    t_arr, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / a.serve_rate)
+        if t > a.serve_seconds:
+            break
+        t_arr.append(t)
+    sizes = np.floor(np.exp(rng.uniform(np.log(1024), np.log(262145), len(t_arr)))).astype(int)
+    jobs = [(nb.plummer(int(n), seed=k) if k % 2 == 0 else nb.disk_bulge(int(n), seed=k))
+            for k, n in enumerate(sizes)]
+    srv = nb.Server(theta=0.6, softening=EPS, dt=1e-3, hbm_budget_bytes=64 << 30,
+                    pool_bodies=1 << 21)
+    t0 = time.perf_counter()
+    k = 0
+    while True:
+        now = time.perf_counter() - t0
+        while k < len(jobs) and t_arr[k] <= now:
+            srv.submit(jobs[k], 100)
+            k += 1
+        r, q = srv.tick()
+        if k == len(jobs) and r == 0 and q == 0:
+            break
+        if r == 0 and q == 0 and k < len(jobs):
+            time.sleep(max(0.0, min(0.01, t_arr[k] - now)))
+        if time.perf_counter() - t0 > a.serve_seconds + 300:
+            break
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    return {"workload": "poisson_jobs_n1024_262144_100_leapfrog_steps",
+            "rate_per_s": a.serve_rate, "arrival_seconds": a.serve_seconds,
+            "jobs": len(jobs), "direct_jobs": int((sizes < 16384).sum()),
+            "jobs_finished": st["jobs_finished"], "wall_s": wall,
+            "step_ms_p50": st["step_ms_p50"], "step_ms_p99": st["step_ms_p99"],
+            "queue_ms_p50": st["queue_ms_p50"], "queue_ms_p99": st["queue_ms_p99"],
+            "ginteractions_s": st["interactions"] / wall / 1e9,
+            "device_busy_fraction": st["busy_ms"] / 1e3 / wall,
+            "max_running": st["max_running"], "peak_device_gb": st["peak_device_bytes"] / 1e9}
+
+
 # ---------------------------------------------------------------- our arm
 def run_ours(a, rank, world, local_rank):
     import numpy as np
@@ -399,6 +492,10 @@ def run_ours(a, rank, world, local_rank):
 
     if not a.skip_extras and rank == 0 and a.bh_steps > 0:
         extras["barnes_hut"] = run_bh(a, nb, torch, dev, stream, flush, np)
+    if not a.skip_extras and rank == 0 and a.ens_steps > 0:
+        extras["ensemble"] = run_ensemble(a, nb, torch, stream)
+    if not a.skip_extras and rank == 0 and a.serve_seconds > 0:
+        extras["serving"] = run_serving(a, nb, np)
 
     # e2e: one force evaluation through the C ABI with pinned host buffers
     e2e = None
