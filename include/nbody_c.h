@@ -129,6 +129,13 @@ nb_status nb_load_device(nb_sim *sim, size_t n, const double *x, const double *y
                          const double *z, const double *vx, const double *vy, const double *vz,
                          const double *m);
 
+/* Makes the simulation work in place on ten caller-owned device arrays of n
+ * doubles (x y z vx vy vz ax ay az m), as the reference's calculators and
+ * integrators work on the caller's ParticleArrays
+ * (CUDA/include/particle_data.hpp:6-43); NULL restores the simulation's own
+ * storage.  The caller keeps the arrays alive while they are bound. */
+nb_status nb_bind_device(nb_sim *sim, size_t n, double *const *arrays10);
+
 /* Copies the state to host arrays; any pointer may be NULL to skip that
  * field.  Replaces copyParticlesToHost (CUDA/src/particle_data.cu:122-143). */
 nb_status nb_read_state(nb_sim *sim, double *x, double *y, double *z, double *vx, double *vy,

@@ -10,6 +10,7 @@
 // on first use.  Everything is enqueued on the simulation's stream.
 #include "nb_internal.h"
 
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -335,6 +336,29 @@ nb_status nb_read_state(nb_sim *s, double *x, double *y, double *z, double *vx, 
             NB_CUDA_TRY(cudaMemcpyAsync(dst[k], s->f[k], bytes, cudaMemcpyDeviceToHost,
                                         s->stream));
     NB_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return NB_OK;
+}
+
+nb_status nb_bind_device(nb_sim *s, size_t n, double *const *arrays10)
+{
+    if (!s) return fail(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+    if (!arrays10) {
+        const size_t ps = plane_stride(s->capacity);
+        for (int k = 0; k < 10; ++k) s->f[k] = s->state.as<double>() + k * ps;
+        s->n = std::min(s->n, s->capacity);
+        s->forces_valid = false;
+        return NB_OK;
+    }
+    if (n > s->capacity) return fail(NB_ERR_CAPACITY, "n exceeds the capacity of the simulation");
+    for (int k = 0; k < 10; ++k)
+        if (n > 0 && !arrays10[k]) return fail(NB_ERR_INVALID_ARGUMENT, "NULL device array");
+    bool same = s->n == n;
+    for (int k = 0; k < 10; ++k) {
+        same = same && s->f[k] == arrays10[k];
+        s->f[k] = arrays10[k];
+    }
+    s->n = n;
+    if (!same) s->forces_valid = false;
     return NB_OK;
 }
 

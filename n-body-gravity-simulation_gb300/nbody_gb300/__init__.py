@@ -36,7 +36,8 @@ STATUS = {0: "NB_OK", 1: "NB_ERR_INVALID_ARGUMENT", 2: "NB_ERR_CUDA", 3: "NB_ERR
 # Every function declared in include/nbody_c.h (checked by the tests).
 EXPORTS = [
     "nb_config_default", "nb_create", "nb_destroy", "nb_set_config", "nb_get_config",
-    "nb_load", "nb_load_device", "nb_read_state", "nb_device_arrays", "nb_num_bodies",
+    "nb_load", "nb_load_device", "nb_bind_device", "nb_read_state", "nb_device_arrays",
+    "nb_num_bodies",
     "nb_compute_forces", "nb_step", "nb_invalidate_forces", "nb_synchronize",
     "nb_diagnostics", "nb_bh_build", "nb_bh_get_info", "nb_bh_read_order", "nb_bh_read_nodes",
     "nb_gen_plummer", "nb_gen_disk_bulge", "nb_status_string", "nb_last_error", "nb_version",
@@ -149,6 +150,7 @@ def lib():
     L.nb_get_config.argtypes = [vp, C.POINTER(_Config)]
     L.nb_load.argtypes = [vp, sz] + [vp] * 7
     L.nb_load_device.argtypes = [vp, sz] + [vp] * 7
+    L.nb_bind_device.argtypes = [vp, sz, vp]
     L.nb_read_state.argtypes = [vp] + [vp] * 10
     L.nb_device_arrays.argtypes = [vp, C.POINTER(vp)]
     L.nb_num_bodies.argtypes = [vp, C.POINTER(sz)]
