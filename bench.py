@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=1.0,
                     help="seconds of Poisson arrivals for the serving extra (0 skips it)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--only", choices=["bh", "ensemble", "serving"], default=None,
+                    help="run one extra workload alone and print its record (profiling)")
     return ap.parse_args()
 
 
@@ -555,11 +557,31 @@ def run_ours(a, rank, world, local_rank):
     return 0
 
 
+def run_only(a, local_rank):
+    import numpy as np
+    import torch
+    import nbody_gb300 as nb
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    if a.only == "bh":
+        flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+        rec = run_bh(a, nb, torch, dev, stream, flush, np)
+    elif a.only == "ensemble":
+        rec = run_ensemble(a, nb, torch, stream)
+    else:
+        rec = run_serving(a, nb, np)
+    print(json.dumps({a.only: rec}), flush=True)
+    return 0
+
+
 def main():
     a = parse()
     rank, world, local_rank = dist_env()
     if a.impl == "reference":
         return run_reference(a, rank, world)
+    if a.only:
+        return run_only(a, local_rank)
     return run_ours(a, rank, world, local_rank)
 
 

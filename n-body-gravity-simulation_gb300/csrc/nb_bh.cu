@@ -108,16 +108,32 @@ bbox_partial_kernel(const double *__restrict__ x, const double *__restrict__ y,
     if (threadIdx.x < 6) part[blockIdx.x * 6 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
-// One thread: the root cube by the CPU tree's rule
-// (force_calculator_barnes_hut_optimized.cpp:112-124, std::max(a,b) = a<b?b:a).
-__global__ void bbox_final_kernel(const double *__restrict__ part, int nparts, BHRoot *root)
+// One block: reduce the partials, then thread 0 derives the root cube by the
+// CPU tree's rule (force_calculator_barnes_hut_optimized.cpp:112-124,
+// std::max(a,b) = a<b?b:a).  Min and max are exact, so the order of the
+// reduction does not matter.
+__global__ void __launch_bounds__(256)
+bbox_final_kernel(const double *__restrict__ part, int nparts, BHRoot *root)
 {
-    if (threadIdx.x != 0) return;
+    __shared__ double sh[6][256];
     double v[6] = {1e308, 1e308, 1e308, -1e308, -1e308, -1e308};
-    for (int b = 0; b < nparts; ++b) {
+    for (int b = threadIdx.x; b < nparts; b += 256) {
         for (int k = 0; k < 3; ++k) v[k] = fmin(v[k], part[b * 6 + k]);
         for (int k = 3; k < 6; ++k) v[k] = fmax(v[k], part[b * 6 + k]);
     }
+    for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = v[k];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            for (int k = 0; k < 3; ++k)
+                sh[k][threadIdx.x] = fmin(sh[k][threadIdx.x], sh[k][threadIdx.x + w]);
+            for (int k = 3; k < 6; ++k)
+                sh[k][threadIdx.x] = fmax(sh[k][threadIdx.x], sh[k][threadIdx.x + w]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    for (int k = 0; k < 6; ++k) v[k] = sh[k][0];
     const double ex = v[3] - v[0], ey = v[4] - v[1], ez = v[5] - v[2];
     const double eyz = (ey < ez) ? ez : ey;
     double size = ((ex < eyz) ? eyz : ex) + 1e-9;
@@ -145,23 +161,76 @@ __global__ void bbox_final_kernel(const double *__restrict__ part, int nparts, B
 }
 
 // ------------------------------------------------------------ Morton encode
+// 21 bits -> every third bit of 63 (standard magic-number spreading).
+__device__ __forceinline__ uint64_t spread21(uint64_t v)
+{
+    v &= 0x1fffffull;
+    v = (v | v << 32) & 0x1f00000000ffffull;
+    v = (v | v << 16) & 0x1f0000ff0000ffull;
+    v = (v | v << 8) & 0x100f00f00f00f00full;
+    v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+    v = (v | v << 2) & 0x1249249249249249ull;
+    return v;
+}
+
+// Fast path of one axis: the cell index on the ideal 2^21 grid of the root
+// cube and whether the position is far enough from every grid line that the
+// CPU tree's rounded running centres cannot compare differently.
+__device__ __forceinline__ bool grid_index(double p, double lo, double scale, double margin,
+                                           uint64_t *q)
+{
+    const double f = (p - lo) * scale;
+    double fl = floor(f);
+    fl = fmin(fmax(fl, 0.0), 2097151.0);
+    *q = (uint64_t)fl;
+    const double d = fmin(f - fl, fl + 1.0 - f);
+    return d > margin;
+}
+
 __global__ void __launch_bounds__(256)
 encode_kernel(const double *__restrict__ x, const double *__restrict__ y,
               const double *__restrict__ z, int n, const BHRoot *__restrict__ root,
               uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
 {
     __shared__ double off[kMaxLevels];
-    __shared__ double c0[3];
+    __shared__ double c0[3], lo[3], scale, margin;
     __shared__ int levels;
     if (threadIdx.x < kMaxLevels) off[threadIdx.x] = root->off[threadIdx.x];
     if (threadIdx.x == 0) {
         c0[0] = root->cx; c0[1] = root->cy; c0[2] = root->cz;
         levels = root->levels;
+        const double size = root->size;
+        double cmax = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = c0[k] - size / 2;
+            cmax = fmax(cmax, fabs(c0[k]));
+        }
+        scale = 2097152.0 / size;
+        // Running centres accumulate at most 21 roundings of half an ulp of
+        // |centre| <= cmax + size; the fast index adds a few more roundings.
+        // Positions farther than this from every grid line index exactly.
+        const double u_c = ldexp(1.0, ilogb(cmax + size) - 52);
+        const double u_s = ldexp(1.0, ilogb(size) - 52);
+        margin = (24.0 * u_c + 4.0 * u_s) * scale + 1e-6;
     }
     __syncthreads();
     const int i = blockIdx.x * 256 + threadIdx.x;
     if (i >= n) return;
     const double px = x[i], py = y[i], pz = z[i];
+    uint64_t qx, qy, qz;
+    const bool okx = grid_index(px, lo[0], scale, margin, &qx);
+    const bool oky = grid_index(py, lo[1], scale, margin, &qy);
+    const bool okz = grid_index(pz, lo[2], scale, margin, &qz);
+    if (okx && oky && okz) {
+        uint64_t code = (spread21(qx) << 2) | (spread21(qy) << 1) | spread21(qz);
+        const int drop = 3 * (kMaxLevels - levels);  // digits below the split limit are 0
+        if (drop >= 63) code = 0;
+        else code = (code >> drop) << drop;
+        keys[i] = code;
+        vals[i] = (uint32_t)i;
+        return;
+    }
+    // Exact path: the CPU tree's own comparisons and child-centre additions.
     double cx = c0[0], cy = c0[1], cz = c0[2];
     uint64_t code = 0;
     for (int l = 0; l < kMaxLevels; ++l) {
@@ -202,31 +271,6 @@ radix_hist_kernel(const uint64_t *__restrict__ keys, int n, int shift, int *__re
     int c = 0;
     for (int w = 0; w < kSortWarps; ++w) c += h[w][threadIdx.x];
     counts[threadIdx.x * num_tiles + blockIdx.x] = c;
-}
-
-// Exclusive scan of an int array in place with one block of 1024 threads.
-__global__ void __launch_bounds__(1024) scan_ints_inplace_kernel(int *__restrict__ a, int len)
-{
-    __shared__ int sh[1024];
-    const int t = threadIdx.x;
-    const int chunk = (len + 1023) / 1024;
-    const int b = t * chunk, e = min(len, b + chunk);
-    int s = 0;
-    for (int k = b; k < e; ++k) s += a[k];
-    sh[t] = s;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const int v = t >= off ? sh[t - off] : 0;
-        __syncthreads();
-        sh[t] += v;
-        __syncthreads();
-    }
-    int run = sh[t] - s;
-    for (int k = b; k < e; ++k) {
-        const int v = a[k];
-        a[k] = run;
-        run += v;
-    }
 }
 
 // Stable scatter of one 8-bit digit.  Warp w of the block ranks keys
@@ -654,7 +698,8 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     NB_TRY(t->keys1.reserve(sizeof(uint64_t) * N));
     NB_TRY(t->vals0.reserve(sizeof(uint32_t) * N));
     NB_TRY(t->vals1.reserve(sizeof(uint32_t) * N));
-    NB_TRY(t->hist.reserve(sizeof(int) * 256 * (size_t)num_tiles));
+    // digit counts per tile, then their exclusive scan (256 * tiles + 1 each)
+    NB_TRY(t->hist.reserve(sizeof(int) * 2 * (256 * (size_t)num_tiles + 1)));
     NB_TRY(t->body.reserve(sizeof(float4) * N));
     NB_TRY(t->moments.reserve(sizeof(D4) * N));
     NB_TRY(t->prefix.reserve(sizeof(D4) * (N + 1)));
@@ -667,7 +712,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
 
     bbox_partial_kernel<<<nparts, 256, 0, st>>>(x, y, z, n, t->part.as<double>());
     NB_LAUNCH_CHECK();
-    bbox_final_kernel<<<1, 32, 0, st>>>(t->part.as<double>(), nparts, root);
+    bbox_final_kernel<<<1, 256, 0, st>>>(t->part.as<double>(), nparts, root);
     NB_LAUNCH_CHECK();
     encode_kernel<<<div_up(n, 256), 256, 0, st>>>(x, y, z, n, root, t->keys0.as<uint64_t>(),
                                                    t->vals0.as<uint32_t>());
@@ -675,14 +720,14 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
 
     uint64_t *kin = t->keys0.as<uint64_t>(), *kout = t->keys1.as<uint64_t>();
     uint32_t *vin = t->vals0.as<uint32_t>(), *vout = t->vals1.as<uint32_t>();
+    int *counts = t->hist.as<int>();
+    int *digit_off = counts + 256 * (size_t)num_tiles + 1;
     for (int shift = 0; shift < 64; shift += 8) {
-        radix_hist_kernel<<<num_tiles, 256, 0, st>>>(kin, n, shift, t->hist.as<int>(),
-                                                     num_tiles);
+        radix_hist_kernel<<<num_tiles, 256, 0, st>>>(kin, n, shift, counts, num_tiles);
         NB_LAUNCH_CHECK();
-        scan_ints_inplace_kernel<<<1, 1024, 0, st>>>(t->hist.as<int>(), 256 * num_tiles);
-        NB_LAUNCH_CHECK();
+        NB_TRY(scan_exclusive<int>(counts, 256 * num_tiles, digit_off, t->scan_tmp, st));
         radix_scatter_kernel<<<num_tiles, 256, 0, st>>>(kin, vin, kout, vout, n, shift,
-                                                        t->hist.as<int>(), num_tiles);
+                                                        digit_off, num_tiles);
         NB_LAUNCH_CHECK();
         std::swap(kin, kout);
         std::swap(vin, vout);
