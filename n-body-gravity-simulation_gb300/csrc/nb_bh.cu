@@ -683,12 +683,12 @@ void bh_destroy(BHTree *t)
     delete t;
 }
 
-nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *z,
-                     const double *m, int n, double G, double eps2, double theta,
-                     int leaf_capacity, double *ax, double *ay, double *az, cudaStream_t st,
-                     const KernelTimer *timer)
+// Root cube, 63-bit codes and the stable LSD sort of the code bits
+// [first_shift, 64) (first_shift 0: the full code).  Leaves the sorted codes
+// and the permutation (sorted index -> original index) in t.
+static nb_status morton_sort(BHTree *t, const double *x, const double *y, const double *z,
+                             int n, int first_shift, cudaStream_t st)
 {
-    if (n <= 0) return NB_OK;
     const size_t N = (size_t)n;
     const int nparts = std::min(div_up(n, 256), 2 * device_props().num_sms);
     const int num_tiles = div_up(n, kSortTile);
@@ -700,15 +700,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     NB_TRY(t->vals1.reserve(sizeof(uint32_t) * N));
     // digit counts per tile, then their exclusive scan (256 * tiles + 1 each)
     NB_TRY(t->hist.reserve(sizeof(int) * 2 * (256 * (size_t)num_tiles + 1)));
-    NB_TRY(t->body.reserve(sizeof(float4) * N));
-    NB_TRY(t->moments.reserve(sizeof(D4) * N));
-    NB_TRY(t->prefix.reserve(sizeof(D4) * (N + 1)));
-    NB_TRY(t->chain_len.reserve(sizeof(int) * N));
-    NB_TRY(t->chain_depth.reserve(sizeof(int) * N));
-    NB_TRY(t->offsets.reserve(sizeof(int) * (N + 1)));
-    NB_TRY(t->stats.reserve(sizeof(BHStats)));
     BHRoot *root = t->root.as<BHRoot>();
-    BHStats *stats = t->stats.as<BHStats>();
 
     bbox_partial_kernel<<<nparts, 256, 0, st>>>(x, y, z, n, t->part.as<double>());
     NB_LAUNCH_CHECK();
@@ -722,7 +714,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     uint32_t *vin = t->vals0.as<uint32_t>(), *vout = t->vals1.as<uint32_t>();
     int *counts = t->hist.as<int>();
     int *digit_off = counts + 256 * (size_t)num_tiles + 1;
-    for (int shift = 0; shift < 64; shift += 8) {
+    for (int shift = first_shift; shift < 64; shift += 8) {
         radix_hist_kernel<<<num_tiles, 256, 0, st>>>(kin, n, shift, counts, num_tiles);
         NB_LAUNCH_CHECK();
         NB_TRY(scan_exclusive<int>(counts, 256 * num_tiles, digit_off, t->scan_tmp, st));
@@ -734,6 +726,43 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     }
     t->sorted_codes = kin;
     t->order = vin;
+    return NB_OK;
+}
+
+nb_status bh_morton_order(BHTree *t, const double *x, const double *y, const double *z, int n,
+                          int levels, cudaStream_t st, const uint32_t **order,
+                          const double **root_centre)
+{
+    if (n <= 0) return NB_OK;
+    levels = std::max(1, std::min(levels, kMaxLevels));
+    // LSD passes over the top 3*levels bits: start at the lowest of them,
+    // rounded down to a digit boundary.
+    const int first_shift = std::max(0, (63 - 3 * levels) / 8 * 8);
+    NB_TRY(morton_sort(t, x, y, z, n, first_shift, st));
+    *order = t->order;
+    *root_centre = &t->root.as<BHRoot>()->cx;
+    return NB_OK;
+}
+
+nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *z,
+                     const double *m, int n, double G, double eps2, double theta,
+                     int leaf_capacity, double *ax, double *ay, double *az, cudaStream_t st,
+                     const KernelTimer *timer)
+{
+    if (n <= 0) return NB_OK;
+    const size_t N = (size_t)n;
+    NB_TRY(t->body.reserve(sizeof(float4) * N));
+    NB_TRY(t->moments.reserve(sizeof(D4) * N));
+    NB_TRY(t->prefix.reserve(sizeof(D4) * (N + 1)));
+    NB_TRY(t->chain_len.reserve(sizeof(int) * N));
+    NB_TRY(t->chain_depth.reserve(sizeof(int) * N));
+    NB_TRY(t->offsets.reserve(sizeof(int) * (N + 1)));
+    NB_TRY(t->stats.reserve(sizeof(BHStats)));
+    NB_TRY(morton_sort(t, x, y, z, n, 0, st));
+    BHRoot *root = t->root.as<BHRoot>();
+    BHStats *stats = t->stats.as<BHStats>();
+    uint64_t *kin = const_cast<uint64_t *>(t->sorted_codes);
+    uint32_t *vin = const_cast<uint32_t *>(t->order);
 
     gather_kernel<<<div_up(n, 256), 256, 0, st>>>(vin, x, y, z, m, n, root,
                                                   t->body.as<float4>(), t->moments.as<D4>());

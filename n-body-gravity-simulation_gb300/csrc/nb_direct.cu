@@ -363,6 +363,11 @@ bool autotune_enabled()
 
 } // namespace
 
+int direct_pick_segments(int iblocks, int tiles, int slots)
+{
+    return pick_segments(iblocks, tiles, slots);
+}
+
 DirectPlan direct_mixed_plan(int n)
 {
     {

@@ -85,6 +85,24 @@ nb_status direct_mixed(const float4 *hi, const float4 *lo, int n, double G, doub
                        cudaStream_t st, const KernelTimer *timer = nullptr,
                        const DirectPlan *plan_override = nullptr);
 DirectPlan direct_mixed_plan(int n);
+// j-split count filling whole waves of `slots` resident CTAs.
+int direct_pick_segments(int iblocks, int tiles, int slots);
+
+// Morton-sorted near/far variant of the mixed path (nb_direct_sorted.cu).
+struct BHTree;
+struct SortedBuffers {
+    DevBuf hi, lo, partials, boxes;
+    BHTree *sorter = nullptr;
+    void release();
+};
+// Bodies are sorted along a Morton curve; every CTA re-centres its j-tiles on
+// its (compact) i-block, and j-tiles farther than the i-block's diameter use
+// the plain FP32 pair term; near tiles keep the double-single one.
+nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
+                              const double *m, int n, double G, double eps2, double *ax,
+                              double *ay, double *az, SortedBuffers &b, cudaStream_t st,
+                              const KernelTimer *timer = nullptr);
+bool direct_sorted_enabled(int n);
 
 // FP64 all-pairs kernel.
 nb_status direct_fp64(const double *x, const double *y, const double *z, const double *m,
@@ -166,6 +184,12 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
                      int leaf_capacity, double *ax, double *ay, double *az, cudaStream_t st,
                      const KernelTimer *timer = nullptr);
 nb_status bh_info(BHTree *t, cudaStream_t st, nb_bh_info *info);
+// Morton order of the bodies by the top 3*levels code bits: *order maps a
+// sorted index to the original one; *root_centre points at the device copy of
+// the root cube centre (3 doubles).  Both stay valid until the next call on t.
+nb_status bh_morton_order(BHTree *t, const double *x, const double *y, const double *z, int n,
+                          int levels, cudaStream_t st, const uint32_t **order,
+                          const double **root_centre);
 nb_status bh_read_order(BHTree *t, cudaStream_t st, uint64_t *codes, uint32_t *order);
 nb_status bh_read_nodes(BHTree *t, cudaStream_t st, int max_nodes, int *depth,
                         uint64_t *prefix, int *first, int *count, int *is_leaf, int *skip,
@@ -187,6 +211,7 @@ struct nb_sim {
     bool forces_valid = false;
 
     nb::DevBuf split_hi, split_lo;   // float4 mirrors for the mixed kernel
+    nb::SortedBuffers sorted;        // Morton-sorted near/far variant of the mixed kernel
     nb::DevBuf partials;             // j-split partial sums
     nb::DevBuf old_acc;              // velocity-Verlet a(t)
     nb::DevBuf rk4;                  // RK4 stage states and accelerations

@@ -107,6 +107,9 @@ nb_status eval_forces(nb_sim *s, const double *px, const double *py, const doubl
         return direct_fp64(px, py, pz, s->m(), n, s->cfg.G, eps2, oax, oay, oaz, s->partials,
                            s->stream, timer);
     case NB_DIRECT_MIXED: {
+        if (direct_sorted_enabled(n))
+            return direct_mixed_sorted(px, py, pz, s->m(), n, s->cfg.G, eps2, oax, oay, oaz,
+                                       s->sorted, s->stream, timer);
         NB_TRY(s->split_hi.reserve(sizeof(float4) * s->capacity));
         NB_TRY(s->split_lo.reserve(sizeof(float4) * s->capacity));
         float4 *hi = s->split_hi.as<float4>(), *lo = s->split_lo.as<float4>();
@@ -266,6 +269,7 @@ nb_status nb_destroy(nb_sim *s)
     s->state.release();
     s->split_hi.release();
     s->split_lo.release();
+    s->sorted.release();
     s->partials.release();
     s->old_acc.release();
     s->rk4.release();

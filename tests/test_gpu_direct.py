@@ -126,6 +126,34 @@ def test_mixed_close_pairs_far_from_origin(nb, oracle):
     check_mixed(oracle, a, ref, st, 1.0, 1e-4)
 
 
+SORTED = ["plummer20000", "diskbulge16384", "cube10000_eps0", "pairs_far_origin_10000"]
+
+
+@pytest.mark.parametrize("name", SORTED)
+def test_mixed_sorted_near_far(nb, oracle, name):
+    """N >= 8192 runs the Morton-sorted near/far variant of the mixed kernel:
+    far j-tiles use FP32 coordinates relative to the i-block centre, near
+    tiles the double-single displacement.  Same tolerances."""
+    G, eps = 1.0, 1e-3
+    if name == "plummer20000":
+        st = nb.plummer(20000, seed=4)
+    elif name == "diskbulge16384":
+        st = nb.disk_bulge(16384, seed=5)
+    elif name == "cube10000_eps0":
+        st, G, eps = cube(oracle, 10000, seed=42), oracle.G_REF, 0.0
+    else:
+        rng = np.random.default_rng(2)
+        c = rng.uniform(-1, 1, size=(5000, 3)) * 1e3
+        p = np.concatenate([c, c + rng.normal(size=(5000, 3)) * 1e-3])
+        z0 = np.zeros(10000)
+        st = (p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy(), z0, z0, z0,
+              rng.uniform(0.5, 2.0, 10000))
+        eps = 1e-4
+    a = gpu_forces(nb, nb.DIRECT_MIXED, st, G, eps)
+    ref = oracle.forces_naive(st[0], st[1], st[2], st[6], G, eps)
+    check_mixed(oracle, a, ref, st, G, eps)
+
+
 @pytest.mark.parametrize("method", ["fp64", "mixed"])
 def test_forces_are_deterministic(nb, oracle, method):
     st = cube(oracle, 3000, seed=9)
