@@ -1,22 +1,38 @@
 // nb_direct_sorted.cu -- the mixed-precision all-pairs sum over Morton-sorted
-// bodies with a near/far split of the j-tiles.
+// bodies with a near/far split decided per warp and per 32-body j-chunk, in
+// packed FP32x2 arithmetic.
 //
-// The double-single displacement of the mixed pair term (nb_pair.cuh) costs 6
-// of its 21 FP32 operations and is needed only when a pair is close compared
-// with the pair's distance from the coordinate origin.  Here the origin is
-// moved to each i-block: bodies are sorted along a Morton curve (the
-// Barnes-Hut encode and radix sort), so the BLOCK*IPT consecutive bodies a CTA
-// owns are spatially compact; the CTA takes the centre c of its i-block's
-// bounding box as origin, and for a j-tile whose bounding box is at least the
-// i-block's diameter D away, forms single-precision coordinates relative to c
-// once per j (when staging the tile) and runs the plain FP32 pair term.
+// Near/far.  The double-single displacement of the mixed pair term costs 6 of
+// its 21 FP32 operations and is needed only when a pair is close compared with
+// the distance of its bodies from the coordinate origin.  Here the origin
+// moves to each warp: bodies are sorted along a Morton curve (the Barnes-Hut
+// encode and radix sort), so the 32*IPT consecutive bodies a warp owns are
+// spatially compact.  The warp takes the centre c of their bounding box as
+// origin and stages every j-chunk (32 consecutive sorted bodies, one per lane)
+// as a normalised double-single (S, E) of x - c.  A chunk whose bounding box
+// lies at least kFarFactor * D from the warp's box (D: the warp box diameter)
+// runs the plain FP32 term on S alone (15 FP32 operations + 1 MUFU); other
+// chunks take the full double-single term on S and E (21 + 1).  Decisions are
+// uniform over the warp (no divergence) and a warp stages its own chunks in its
+// own shared memory: no CTA-wide barrier.
 //
-// Error of the far term: |xi - c| <= D/2 and |xj - c| <= r + D/2, so the
-// rounding of the relative coordinates is at most 2^-24 (r + D) <= 2^-23 r
-// for r >= D -- a displacement good to ~1.2e-7 relative, like the FP32
-// arithmetic that follows.  The folded Newton step on the MUFU rsqrt is kept.
-// Near tiles (including the i-block's own) take the full double-single term.
-// Every tile decision is uniform over the CTA, so there is no divergence.
+// Packed arithmetic.  sm_100-class SMs execute FP32 add, multiply and FMA on
+// register pairs (f32x2) at the FP32 pipe's lane rate but half the issue
+// slots.  The scalar kernels issue ~24 instructions per interaction for 21 FP32
+// operations and sit at the issue limit; here each thread evaluates two j at
+// once (a j-pair, staged side by side in shared memory) against IPT i-bodies
+// held as duplicated pairs, so the FP32 work issues as f32x2 and the FP32 pipe,
+// not issue, bounds the kernel.  Every lane of an f32x2 operation rounds like
+// its scalar counterpart.
+//
+// Error of a far term: S carries one FP32 rounding of x - c.  With
+// |xi - c| <= D/2, |xj - c| <= r + D/2 and the subtraction's own rounding, the
+// displacement error is at most 2^-24 (2r + D) <= 2^-24 r (2 + 1/kFarFactor)
+// = 2^-22 r for kFarFactor = 1/2 -- about 2.4e-7 relative, the same order as
+// the FP32 arithmetic of the term.  Near terms keep the double-single
+// displacement (absolute error ~2^-48 |x|).  The folded Newton step on the
+// MUFU rsqrt is kept; every FP32 accumulator takes 32 terms before its
+// Kahan-compensated add, and the segments combine in FP64.
 #include "nb_internal.h"
 #include "nb_pair.cuh"
 
@@ -28,6 +44,9 @@
 
 namespace nb {
 namespace {
+
+constexpr int kChunk = 32;             // j-chunk = one body per lane
+constexpr float kFarFactor2 = 0.25f;   // (gap / D)^2 threshold: kFarFactor = 1/2
 
 // Positions in Morton order relative to the root centre, split into
 // double-single hi/lo parts; mass in hi.w.
@@ -47,171 +66,239 @@ __global__ void split_sorted_kernel(const uint32_t *__restrict__ order,
                         __double2float_rn(Z - (double)hz), 0.0f);
 }
 
-// Bounding box of every tile of `tile` consecutive sorted bodies (one block
-// of `tile` threads per tile): box[2t] = min, box[2t+1] = max.
-__global__ void tile_box_kernel(const float4 *__restrict__ hi, int n, float4 *__restrict__ box)
+// Bounding box of every chunk of 32 consecutive sorted bodies (one warp per
+// chunk): box[2t] = min, box[2t+1] = max.  Lanes past n repeat the chunk's
+// first body, which is valid.
+__global__ void chunk_box_kernel(const float4 *__restrict__ hi, int n, int nchunks,
+                                 float4 *__restrict__ box)
 {
-    __shared__ float mn[3][256], mx[3][256];
-    const int t = threadIdx.x, tile = blockDim.x;
-    const int i = blockIdx.x * tile + t;
-    float4 p = i < n ? hi[i] : hi[blockIdx.x * tile];  // the tile's first body is valid
-    mn[0][t] = mx[0][t] = p.x;
-    mn[1][t] = mx[1][t] = p.y;
-    mn[2][t] = mx[2][t] = p.z;
-    __syncthreads();
-    for (int w = tile / 2; w > 0; w >>= 1) {
-        if (t < w)
-            for (int k = 0; k < 3; ++k) {
-                mn[k][t] = fminf(mn[k][t], mn[k][t + w]);
-                mx[k][t] = fmaxf(mx[k][t], mx[k][t + w]);
-            }
-        __syncthreads();
-    }
-    if (t == 0) {
-        box[2 * blockIdx.x] = make_float4(mn[0][0], mn[1][0], mn[2][0], 0.f);
-        box[2 * blockIdx.x + 1] = make_float4(mx[0][0], mx[1][0], mx[2][0], 0.f);
-    }
-}
-
-// Plain FP32 pair term on coordinates relative to the i-block centre.
-template <bool ZERO_SOFT>
-__device__ __forceinline__ void pair_term_far(const float4 &A, float xr, float yr, float zr,
-                                              float eps2, float &ax, float &ay, float &az)
-{
-    const float dx = A.x - xr;
-    const float dy = A.y - yr;
-    const float dz = A.z - zr;
-    const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-    float inv = rsqrt_mufu(r2);
-    if (ZERO_SOFT) inv = (r2 > 0.f) ? inv : 0.f;
-    const float inv2 = inv * inv;
-    const float corr = fmaf(-1.5f, r2 * inv2, 2.5f);
-    const float s = ((A.w * inv) * inv2) * corr;
-    ax = fmaf(dx, s, ax);
-    ay = fmaf(dy, s, ay);
-    az = fmaf(dz, s, az);
-}
-
-template <int BLOCK, int IPT, bool ZERO_SOFT>
-__global__ void __launch_bounds__(BLOCK)
-direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
-                     const float4 *__restrict__ box, int n, int ntiles, float eps2,
-                     int seg_len, float *__restrict__ psum, float *__restrict__ pcomp,
-                     unsigned long long *__restrict__ far_tiles)
-{
-    __shared__ float4 sh_a[BLOCK];
-    __shared__ float4 sh_b[BLOCK];
-    __shared__ float s_geo[10];  // i-box min xyz, max xyz, centre xyz, diameter^2
-
-    const int tid = threadIdx.x;
-    const int ibase = blockIdx.x * (BLOCK * IPT);
-    if (tid == 0) {
-        float mn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, mx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
-        const int t0 = ibase / BLOCK;
-        for (int k = 0; k < IPT && t0 + k < ntiles; ++k) {
-            const float4 a = box[2 * (t0 + k)], b = box[2 * (t0 + k) + 1];
-            mn[0] = fminf(mn[0], a.x); mn[1] = fminf(mn[1], a.y); mn[2] = fminf(mn[2], a.z);
-            mx[0] = fmaxf(mx[0], b.x); mx[1] = fmaxf(mx[1], b.y); mx[2] = fmaxf(mx[2], b.z);
-        }
-        float d2 = 0.f;
+    const int t = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (t >= nchunks) return;
+    const int i = t * kChunk + lane;
+    const float4 p = hi[i < n ? i : t * kChunk];
+    float mn[3] = {p.x, p.y, p.z}, mx[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
         for (int k = 0; k < 3; ++k) {
-            s_geo[k] = mn[k];
-            s_geo[3 + k] = mx[k];
-            s_geo[6 + k] = 0.5f * (mn[k] + mx[k]);
-            d2 += (mx[k] - mn[k]) * (mx[k] - mn[k]);
+            mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+            mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
         }
-        s_geo[9] = d2;
+    if (lane == 0) {
+        box[2 * t] = make_float4(mn[0], mn[1], mn[2], 0.f);
+        box[2 * t + 1] = make_float4(mx[0], mx[1], mx[2], 0.f);
     }
-    __syncthreads();
-    const float cx = s_geo[6], cy = s_geo[7], cz = s_geo[8], diam2 = s_geo[9];
+}
 
-    float xh[IPT], yh[IPT], zh[IPT], xl[IPT], yl[IPT], zl[IPT], xr[IPT], yr[IPT], zr[IPT];
+// s + e = a + b exactly (Knuth's two-sum; plain adds, nothing to contract).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// (h + l) - c as a normalised double-single S + E (|E| <= ulp(S) / 2); the
+// only rounding is that of the low-order add, ~2^-48 |h|.
+__device__ __forceinline__ void rel_ds(float h, float l, float c, float &S, float &E)
+{
+    float s, e;
+    two_sum(h, -c, s, e);
+    two_sum(s, e + l, S, E);
+}
+
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+
+// m r^-3 of a j-pair with the folded Newton step; ZERO_SOFT zeroes the
+// r2 == 0 (j == i) lane.
+template <bool ZERO_SOFT>
+__device__ __forceinline__ float2 pair_scale(float2 r2, float2 m)
+{
+    float2 inv = make_float2(rsqrt_mufu(r2.x), rsqrt_mufu(r2.y));
+    if (ZERO_SOFT) {
+        inv.x = r2.x > 0.f ? inv.x : 0.f;
+        inv.y = r2.y > 0.f ? inv.y : 0.f;
+    }
+    const float2 inv2 = mul2(inv, inv);
+    const float2 corr = fma2(dup2(-1.5f), mul2(r2, inv2), dup2(2.5f));
+    return mul2(mul2(mul2(m, inv), inv2), corr);
+}
+
+// One warp's staged j-chunk: j-pair p (bodies 2p and 2p+1 of the chunk) side
+// by side, so that one broadcast 16-byte load gives two f32x2 operands.
+struct ChunkStage {
+    float4 s[kChunk / 2];  // (Sx_2p, Sx_2p+1, Sy_2p, Sy_2p+1)
+    float4 t[kChunk / 2];  // (Sz_2p, Sz_2p+1, m_2p, m_2p+1)
+    float4 e[kChunk / 2];  // (Ex_2p, Ex_2p+1, Ey_2p, Ey_2p+1)
+    float2 f[kChunk / 2];  // (Ez_2p, Ez_2p+1)
+};
+
+// One warp = 32*IPT consecutive sorted i-bodies (chunks tile0 .. tile0+IPT-1,
+// lane l of chunk k holds body (tile0 + k) * 32 + l); blockIdx.y selects the
+// j-chunks [y * seg_chunks, (y + 1) * seg_chunks).  Writes per-segment Kahan
+// sums and compensations (sorted order).  Warps are independent: a warp whose
+// chunks are all past n returns at once.
+template <int WARPS, int IPT, bool ZERO_SOFT>
+__global__ void __launch_bounds__(WARPS * 32)
+direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+                     const float4 *__restrict__ box, int n, int nchunks, float eps2,
+                     int seg_chunks, float *__restrict__ psum, float *__restrict__ pcomp)
+{
+    __shared__ ChunkStage stage[WARPS];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int tile0 = (blockIdx.x * WARPS + w) * IPT;
+    if (tile0 >= nchunks) return;
+    ChunkStage &sg = stage[w];
+
+    // the warp's box: union of its chunk boxes; centre and far threshold
+    float bmn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, bmx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+#pragma unroll
+    for (int k = 0; k < IPT; ++k)
+        if (tile0 + k < nchunks) {
+            const float4 a = box[2 * (tile0 + k)], b = box[2 * (tile0 + k) + 1];
+            bmn[0] = fminf(bmn[0], a.x); bmn[1] = fminf(bmn[1], a.y); bmn[2] = fminf(bmn[2], a.z);
+            bmx[0] = fmaxf(bmx[0], b.x); bmx[1] = fmaxf(bmx[1], b.y); bmx[2] = fmaxf(bmx[2], b.z);
+        }
+    const float cx = 0.5f * (bmn[0] + bmx[0]), cy = 0.5f * (bmn[1] + bmx[1]),
+                cz = 0.5f * (bmn[2] + bmx[2]);
+    const float thr2 = kFarFactor2 * ((bmx[0] - bmn[0]) * (bmx[0] - bmn[0]) +
+                                      (bmx[1] - bmn[1]) * (bmx[1] - bmn[1]) +
+                                      (bmx[2] - bmn[2]) * (bmx[2] - bmn[2]));
+
+    // i-bodies relative to c, negated and duplicated into pairs
+    float2 nsx[IPT], nsy[IPT], nsz[IPT], nex[IPT], ney[IPT], nez[IPT];
     float sx[IPT], sy[IPT], sz[IPT], qx[IPT], qy[IPT], qz[IPT];
+    float2 ax[IPT], ay[IPT], az[IPT];
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
-        const int i = ibase + k * BLOCK + tid;
+        const int i = (tile0 + k) * kChunk + lane;
         float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
         if (i < n) {
             h = hi[i];
             l = lo[i];
         }
-        xh[k] = h.x; yh[k] = h.y; zh[k] = h.z;
-        xl[k] = l.x; yl[k] = l.y; zl[k] = l.z;
-        xr[k] = (h.x - cx) + l.x;
-        yr[k] = (h.y - cy) + l.y;
-        zr[k] = (h.z - cz) + l.z;
+        float S, E;
+        rel_ds(h.x, l.x, cx, S, E);
+        nsx[k] = dup2(-S);
+        nex[k] = dup2(-E);
+        rel_ds(h.y, l.y, cy, S, E);
+        nsy[k] = dup2(-S);
+        ney[k] = dup2(-E);
+        rel_ds(h.z, l.z, cz, S, E);
+        nsz[k] = dup2(-S);
+        nez[k] = dup2(-E);
         sx[k] = sy[k] = sz[k] = 0.f;
         qx[k] = qy[k] = qz[k] = 0.f;
+        ax[k] = ay[k] = az[k] = dup2(0.f);
     }
+    const float2 e2 = dup2(eps2);
 
-    unsigned nfar = 0;
-    const int j0 = blockIdx.y * seg_len;
-    const int j1 = min(n, j0 + seg_len);
-    for (int t0 = j0; t0 < j1; t0 += BLOCK) {
-        // tile gap to the i-block box: far when at least the i-block diameter
-        const float4 bmin = box[2 * (t0 / BLOCK)], bmax = box[2 * (t0 / BLOCK) + 1];
-        const float gx = fmaxf(0.f, fmaxf(bmin.x - s_geo[3], s_geo[0] - bmax.x));
-        const float gy = fmaxf(0.f, fmaxf(bmin.y - s_geo[4], s_geo[1] - bmax.y));
-        const float gz = fmaxf(0.f, fmaxf(bmin.z - s_geo[5], s_geo[2] - bmax.z));
+    const int jc0 = blockIdx.y * seg_chunks;
+    const int jc1 = min(nchunks, jc0 + seg_chunks);
+    // the lane's body of the next chunk, loaded one chunk ahead
+    float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
+    bool valid = jc0 < jc1 && jc0 * kChunk + lane < n;
+    if (valid) {
+        h = hi[jc0 * kChunk + lane];
+        l = lo[jc0 * kChunk + lane];
+    }
+    int pending = 0;  // chunks in the FP32 accumulators since the last Kahan add
+    float *const s_s = reinterpret_cast<float *>(&sg.s[lane >> 1]) + (lane & 1);
+    float *const s_t = reinterpret_cast<float *>(&sg.t[lane >> 1]) + (lane & 1);
+    float *const s_e = reinterpret_cast<float *>(&sg.e[lane >> 1]) + (lane & 1);
+    float *const s_f = reinterpret_cast<float *>(&sg.f[lane >> 1]) + (lane & 1);
+    for (int jc = jc0; jc < jc1; ++jc) {
+        const float4 jmn = box[2 * jc], jmx = box[2 * jc + 1];
+        const float gx = fmaxf(0.f, fmaxf(jmn.x - bmx[0], bmn[0] - jmx.x));
+        const float gy = fmaxf(0.f, fmaxf(jmn.y - bmx[1], bmn[1] - jmx.y));
+        const float gz = fmaxf(0.f, fmaxf(jmn.z - bmx[2], bmn[2] - jmx.z));
         const float gap2 = gx * gx + gy * gy + gz * gz;
-        const bool far = gap2 > 0.f && gap2 >= diam2;
-        nfar += far;
+        const bool far = gap2 > 0.f && gap2 >= thr2;
 
-        const int j = t0 + tid;
-        float4 h = far_body(), l = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (j < j1) {
-            h = hi[j];
-            l = lo[j];
+        // lanes past n stage a massless body far away: its terms are exactly 0
+        float Sx = 1.0e18f, Sy = 1.0e18f, Sz = 1.0e18f, Ex = 0.f, Ey = 0.f, Ez = 0.f, mj = 0.f;
+        if (valid) {
+            rel_ds(h.x, l.x, cx, Sx, Ex);
+            rel_ds(h.y, l.y, cy, Sy, Ey);
+            rel_ds(h.z, l.z, cz, Sz, Ez);
+            mj = h.w;
         }
-        __syncthreads();
-        if (far) sh_a[tid] = make_float4((h.x - cx) + l.x, (h.y - cy) + l.y, (h.z - cz) + l.z, h.w);
-        else {
-            sh_a[tid] = h;
-            sh_b[tid] = l;
+        __syncwarp();
+        s_s[0] = Sx;
+        s_s[2] = Sy;
+        s_t[0] = Sz;
+        s_t[2] = mj;
+        s_e[0] = Ex;
+        s_e[2] = Ey;
+        s_f[0] = Ez;
+        __syncwarp();
+        valid = jc + 1 < jc1 && (jc + 1) * kChunk + lane < n;
+        if (valid) {
+            h = hi[(jc + 1) * kChunk + lane];
+            l = lo[(jc + 1) * kChunk + lane];
         }
-        __syncthreads();
 
-        constexpr int kSub = 32;
-#pragma unroll 1
-        for (int s0 = 0; s0 < BLOCK; s0 += kSub) {
-            float ax[IPT], ay[IPT], az[IPT];
-#pragma unroll
-            for (int k = 0; k < IPT; ++k) ax[k] = ay[k] = az[k] = 0.f;
-            if (far) {
+        if (far) {
 #pragma unroll 4
-                for (int jj = s0; jj < s0 + kSub; ++jj) {
-                    const float4 A = sh_a[jj];
+            for (int p = 0; p < kChunk / 2; ++p) {
+                const float4 A = sg.s[p], B = sg.t[p];
+                const float2 X = make_float2(A.x, A.y), Y = make_float2(A.z, A.w);
+                const float2 Z = make_float2(B.x, B.y), M = make_float2(B.z, B.w);
 #pragma unroll
-                    for (int k = 0; k < IPT; ++k)
-                        pair_term_far<ZERO_SOFT>(A, xr[k], yr[k], zr[k], eps2, ax[k], ay[k],
-                                                 az[k]);
-                }
-            } else {
-#pragma unroll 4
-                for (int jj = s0; jj < s0 + kSub; ++jj) {
-                    const float4 H = sh_a[jj];
-                    const float4 L = sh_b[jj];
-#pragma unroll
-                    for (int k = 0; k < IPT; ++k)
-                        pair_term<ZERO_SOFT>(H, L, xh[k], yh[k], zh[k], xl[k], yl[k], zl[k], eps2,
-                                             ax[k], ay[k], az[k]);
+                for (int k = 0; k < IPT; ++k) {
+                    const float2 dx = add2(X, nsx[k]);
+                    const float2 dy = add2(Y, nsy[k]);
+                    const float2 dz = add2(Z, nsz[k]);
+                    const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+                    const float2 s = pair_scale<false>(r2, M);
+                    ax[k] = fma2(dx, s, ax[k]);
+                    ay[k] = fma2(dy, s, ay[k]);
+                    az[k] = fma2(dz, s, az[k]);
                 }
             }
+        } else {
+#pragma unroll 2
+            for (int p = 0; p < kChunk / 2; ++p) {
+                const float4 A = sg.s[p], B = sg.t[p], C = sg.e[p];
+                const float2 F = sg.f[p];
+                const float2 X = make_float2(A.x, A.y), Y = make_float2(A.z, A.w);
+                const float2 Z = make_float2(B.x, B.y), M = make_float2(B.z, B.w);
+                const float2 EX = make_float2(C.x, C.y), EY = make_float2(C.z, C.w);
+#pragma unroll
+                for (int k = 0; k < IPT; ++k) {
+                    const float2 dx = add2(add2(X, nsx[k]), add2(EX, nex[k]));
+                    const float2 dy = add2(add2(Y, nsy[k]), add2(EY, ney[k]));
+                    const float2 dz = add2(add2(Z, nsz[k]), add2(F, nez[k]));
+                    const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+                    const float2 s = pair_scale<ZERO_SOFT>(r2, M);
+                    ax[k] = fma2(dx, s, ax[k]);
+                    ay[k] = fma2(dy, s, ay[k]);
+                    az[k] = fma2(dz, s, az[k]);
+                }
+            }
+        }
+        // every accumulator lane holds 16 terms per chunk: fold after two
+        if (++pending == 2 || jc + 1 == jc1) {
 #pragma unroll
             for (int k = 0; k < IPT; ++k) {
-                kahan_add(sx[k], qx[k], ax[k]);
-                kahan_add(sy[k], qy[k], ay[k]);
-                kahan_add(sz[k], qz[k], az[k]);
+                kahan_add(sx[k], qx[k], ax[k].x + ax[k].y);
+                kahan_add(sy[k], qy[k], ay[k].x + ay[k].y);
+                kahan_add(sz[k], qz[k], az[k].x + az[k].y);
+                ax[k] = ay[k] = az[k] = dup2(0.f);
             }
+            pending = 0;
         }
     }
-    if (far_tiles && tid == 0 && nfar) atomicAdd(far_tiles, (unsigned long long)nfar);
 
     const size_t plane = (size_t)n;
     const size_t base = (size_t)blockIdx.y * 3 * plane;
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
-        const int i = ibase + k * BLOCK + tid;
+        const int i = (tile0 + k) * kChunk + lane;
         if (i < n) {
             psum[base + i] = sx[k];
             psum[base + plane + i] = sy[k];
@@ -247,78 +334,82 @@ __global__ void combine_sorted_kernel(const float *__restrict__ psum,
 }
 
 struct SortedShape {
-    int block, ipt;
+    int warps, ipt;
 };
-constexpr SortedShape kSortedShapes[] = {{256, 4}, {128, 8}, {128, 4}};
+constexpr SortedShape kSortedShapes[] = {{4, 4}, {8, 4}, {4, 2}, {8, 2}};
 constexpr int kNumSortedShapes = sizeof(kSortedShapes) / sizeof(kSortedShapes[0]);
 
-template <int B, int I>
+template <int W, int I>
 int sorted_slots()
 {
     static int slots = 0;
     if (!slots) {
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, (const void *)direct_sorted_kernel<B, I, false>, B, 0);
+            &per_sm, (const void *)direct_sorted_kernel<W, I, false>, W * 32, 0);
         slots = std::max(1, per_sm) * device_props().num_sms;
     }
     return slots;
 }
 
-int sorted_slots_for(int block, int ipt)
+int sorted_slots_for(int warps, int ipt)
 {
-    if (block == 256 && ipt == 4) return sorted_slots<256, 4>();
-    if (block == 128 && ipt == 8) return sorted_slots<128, 8>();
-    if (block == 128 && ipt == 4) return sorted_slots<128, 4>();
+    if (warps == 4 && ipt == 4) return sorted_slots<4, 4>();
+    if (warps == 8 && ipt == 4) return sorted_slots<8, 4>();
+    if (warps == 4 && ipt == 2) return sorted_slots<4, 2>();
+    if (warps == 8 && ipt == 2) return sorted_slots<8, 2>();
     return 0;
 }
 
-template <int B, int I>
+template <int W, int I>
 void launch_sorted_shape(dim3 grid, cudaStream_t st, const float4 *hi, const float4 *lo,
-                         const float4 *box, int n, double eps2, int seg_len, float *psum,
-                         float *pcomp, unsigned long long *far_tiles)
+                         const float4 *box, int n, double eps2, int seg_chunks, float *psum,
+                         float *pcomp)
 {
-    const int ntiles = (n + B - 1) / B;
+    const int nchunks = (n + kChunk - 1) / kChunk;
     if (eps2 > 0.0)
-        direct_sorted_kernel<B, I, false><<<grid, B, 0, st>>>(hi, lo, box, n, ntiles, (float)eps2,
-                                                              seg_len, psum, pcomp, far_tiles);
+        direct_sorted_kernel<W, I, false><<<grid, W * 32, 0, st>>>(
+            hi, lo, box, n, nchunks, (float)eps2, seg_chunks, psum, pcomp);
     else
-        direct_sorted_kernel<B, I, true><<<grid, B, 0, st>>>(hi, lo, box, n, ntiles, 0.0f,
-                                                             seg_len, psum, pcomp, far_tiles);
+        direct_sorted_kernel<W, I, true><<<grid, W * 32, 0, st>>>(
+            hi, lo, box, n, nchunks, 0.0f, seg_chunks, psum, pcomp);
 }
 
+// DirectPlan fields here: block = threads per CTA (32 * warps), ipt = chunks
+// per warp, seg_tiles = j-chunks per segment.
 bool launch_sorted(const DirectPlan &p, cudaStream_t st, const float4 *hi, const float4 *lo,
-                   const float4 *box, int n, double eps2, float *psum, float *pcomp,
-                   unsigned long long *far_tiles)
+                   const float4 *box, int n, double eps2, float *psum, float *pcomp)
 {
-    const int per_cta = p.block * p.ipt;
-    dim3 grid((n + per_cta - 1) / per_cta, p.segments);
-    const int seg_len = p.seg_tiles * p.block;
-    if (p.block == 256 && p.ipt == 4)
-        launch_sorted_shape<256, 4>(grid, st, hi, lo, box, n, eps2, seg_len, psum, pcomp,
-                                    far_tiles);
-    else if (p.block == 128 && p.ipt == 8)
-        launch_sorted_shape<128, 8>(grid, st, hi, lo, box, n, eps2, seg_len, psum, pcomp,
-                                    far_tiles);
-    else if (p.block == 128 && p.ipt == 4)
-        launch_sorted_shape<128, 4>(grid, st, hi, lo, box, n, eps2, seg_len, psum, pcomp,
-                                    far_tiles);
+    const int warps = p.block / 32;
+    const int nchunks = (n + kChunk - 1) / kChunk;
+    const int per_cta = warps * p.ipt;
+    const dim3 grid((nchunks + per_cta - 1) / per_cta, p.segments);
+    if (warps == 4 && p.ipt == 4)
+        launch_sorted_shape<4, 4>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
+    else if (warps == 8 && p.ipt == 4)
+        launch_sorted_shape<8, 4>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
+    else if (warps == 4 && p.ipt == 2)
+        launch_sorted_shape<4, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
+    else if (warps == 8 && p.ipt == 2)
+        launch_sorted_shape<8, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
     else
         return false;
     return true;
 }
 
-DirectPlan sorted_plan_for_shape(int n, int block, int ipt)
+DirectPlan sorted_plan_for_shape(int n, int warps, int ipt)
 {
     DirectPlan p;
-    p.block = block;
+    p.block = warps * 32;
     p.ipt = ipt;
-    const int per_cta = block * ipt;
-    const int iblocks = (n + per_cta - 1) / per_cta;
-    const int tiles = (n + block - 1) / block;
-    p.segments = direct_pick_segments(iblocks, tiles, sorted_slots_for(block, ipt));
-    p.seg_tiles = (tiles + p.segments - 1) / p.segments;
-    p.segments = (tiles + p.seg_tiles - 1) / p.seg_tiles;
+    const int nchunks = (n + kChunk - 1) / kChunk;
+    const int per_cta = warps * ipt;
+    const int iblocks = (nchunks + per_cta - 1) / per_cta;
+    // segments of at least 8 chunks (256 j)
+    const int units = std::max(1, nchunks / 8);
+    const int s = direct_pick_segments(iblocks, units, sorted_slots_for(warps, ipt));
+    p.seg_tiles = (nchunks + s - 1) / s;
+    p.segments = (nchunks + p.seg_tiles - 1) / p.seg_tiles;
     return p;
 }
 
@@ -346,18 +437,13 @@ bool direct_sorted_enabled(int n)
     return on && n >= 8192;
 }
 
-// Boxes of tiles of the plan's block size, then the kernel.
 static nb_status run_sorted(const DirectPlan &p, const float4 *hi, const float4 *lo, int n,
                             double eps2, SortedBuffers &b, cudaStream_t st, float **psum_out)
 {
-    const int ntiles = (n + p.block - 1) / p.block;
-    NB_TRY(b.boxes.reserve(sizeof(float4) * 2 * (size_t)ntiles));
     NB_TRY(b.partials.reserve(sizeof(float) * 6 * (size_t)n * p.segments));
-    tile_box_kernel<<<ntiles, p.block, 0, st>>>(hi, n, b.boxes.as<float4>());
-    NB_LAUNCH_CHECK();
     float *psum = b.partials.as<float>();
     float *pcomp = psum + 3 * (size_t)n * p.segments;
-    if (!launch_sorted(p, st, hi, lo, b.boxes.as<float4>(), n, eps2, psum, pcomp, nullptr))
+    if (!launch_sorted(p, st, hi, lo, b.boxes.as<float4>(), n, eps2, psum, pcomp))
         return fail(NB_ERR_UNSUPPORTED, "direct_mixed_sorted: unsupported tile shape");
     NB_LAUNCH_CHECK();
     *psum_out = psum;
@@ -372,7 +458,7 @@ static nb_status autotune_sorted(const float4 *hi, const float4 *lo, int n, doub
     NB_CUDA_TRY(cudaEventCreate(&e1));
     float best_ms = 1e30f;
     for (int k = 0; k < kNumSortedShapes; ++k) {
-        const DirectPlan p = sorted_plan_for_shape(n, kSortedShapes[k].block, kSortedShapes[k].ipt);
+        const DirectPlan p = sorted_plan_for_shape(n, kSortedShapes[k].warps, kSortedShapes[k].ipt);
         float *psum = nullptr;
         NB_TRY(run_sorted(p, hi, lo, n, eps2, b, st, &psum));
         cudaEventRecord(e0, st);
@@ -401,12 +487,16 @@ nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
     if (!b.sorter) b.sorter = bh_create();
     const uint32_t *order = nullptr;
     const double *centre = nullptr;
-    // 10 levels of the Morton curve: cells far smaller than an i-block
+    // 10 levels of the Morton curve: cells far smaller than a 32-body chunk
     NB_TRY(bh_morton_order(b.sorter, x, y, z, n, 10, st, &order, &centre));
+    const int nchunks = (n + kChunk - 1) / kChunk;
     NB_TRY(b.hi.reserve(sizeof(float4) * (size_t)n));
     NB_TRY(b.lo.reserve(sizeof(float4) * (size_t)n));
+    NB_TRY(b.boxes.reserve(sizeof(float4) * 2 * (size_t)nchunks));
     float4 *hi = b.hi.as<float4>(), *lo = b.lo.as<float4>();
     split_sorted_kernel<<<(n + 255) / 256, 256, 0, st>>>(order, x, y, z, m, n, centre, hi, lo);
+    NB_LAUNCH_CHECK();
+    chunk_box_kernel<<<(nchunks + 7) / 8, 256, 0, st>>>(hi, n, nchunks, b.boxes.as<float4>());
     NB_LAUNCH_CHECK();
     DirectPlan p;
     bool tuned;
@@ -419,7 +509,7 @@ nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
     if (!tuned) {
         const char *e = std::getenv("NB_AUTOTUNE");
         if (!(e && std::strcmp(e, "0") == 0)) NB_TRY(autotune_sorted(hi, lo, n, eps2, b, st, &p));
-        else p = sorted_plan_for_shape(n, 256, 4);
+        else p = sorted_plan_for_shape(n, 4, 4);
     }
     if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
     float *psum = nullptr;

@@ -95,9 +95,10 @@ struct SortedBuffers {
     BHTree *sorter = nullptr;
     void release();
 };
-// Bodies are sorted along a Morton curve; every CTA re-centres its j-tiles on
-// its (compact) i-block, and j-tiles farther than the i-block's diameter use
-// the plain FP32 pair term; near tiles keep the double-single one.
+// Bodies are sorted along a Morton curve; every warp re-centres the j-chunks
+// (32 bodies) that lie at least half its (compact) i-box diameter away on its
+// own box and runs the plain FP32 pair term on them; near chunks keep the
+// double-single one.
 nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
                               const double *m, int n, double G, double eps2, double *ax,
                               double *ay, double *az, SortedBuffers &b, cudaStream_t st,
