@@ -10,8 +10,9 @@
 // are ordered by cost, largest first.  A persistent kernel (a fixed grid of
 // resident CTAs) lets every warp take the next item with one atomicAdd and
 // sum its system's j-bodies in tiles of 32 staged in the warp's own slice of
-// shared memory: the same double-single / folded-Newton pair term and 32-term
-// Kahan grouping as the single-system kernel.  Each item writes only its own
+// shared memory: the same double-single / folded-Newton pair term as the
+// single-system kernel, evaluated on j-pairs in packed f32x2 arithmetic, and a
+// Kahan-compensated add after every tile.  Each item writes only its own
 // i-bodies' accelerations, after summing j in index order, so a system's
 // result does not depend on what else is in the batch or on which warp ran
 // which item: a system gives the same bits alone and in any mix.
@@ -35,10 +36,11 @@ __device__ __forceinline__ void batch_item(const float4 *__restrict__ hi,
                                            const float4 *__restrict__ lo, const SysDesc &sd,
                                            int i0, float eps2, double G, double *__restrict__ ax,
                                            double *__restrict__ ay, double *__restrict__ az,
-                                           float4 *sh_hi, float4 *sh_lo)
+                                           PairTile &pt)
 {
     const int lane = threadIdx.x & 31;
-    float xh[IPT], yh[IPT], zh[IPT], xl[IPT], yl[IPT], zl[IPT];
+    // i-bodies negated and duplicated into f32x2 pairs
+    float2 nxh[IPT], nyh[IPT], nzh[IPT], nxl[IPT], nyl[IPT], nzl[IPT];
     float sx[IPT], sy[IPT], sz[IPT], cx[IPT], cy[IPT], cz[IPT];
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
@@ -48,11 +50,12 @@ __device__ __forceinline__ void batch_item(const float4 *__restrict__ hi,
             h = hi[sd.first + i];
             l = lo[sd.first + i];
         }
-        xh[k] = h.x; yh[k] = h.y; zh[k] = h.z;
-        xl[k] = l.x; yl[k] = l.y; zl[k] = l.z;
+        nxh[k] = dup2(-h.x); nyh[k] = dup2(-h.y); nzh[k] = dup2(-h.z);
+        nxl[k] = dup2(-l.x); nyl[k] = dup2(-l.y); nzl[k] = dup2(-l.z);
         sx[k] = sy[k] = sz[k] = 0.f;
         cx[k] = cy[k] = cz[k] = 0.f;
     }
+    const float2 e2 = dup2(eps2);
     for (int t0 = 0; t0 < sd.n; t0 += 32) {
         const int j = t0 + lane;
         float4 h = far_body(), l = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -61,26 +64,24 @@ __device__ __forceinline__ void batch_item(const float4 *__restrict__ hi,
             l = lo[sd.first + j];
         }
         __syncwarp();
-        sh_hi[lane] = h;
-        sh_lo[lane] = l;
+        pair_tile_put(pt, lane, h.x, h.y, h.z, h.w, l.x, l.y, l.z);
         __syncwarp();
-        float ax_[IPT], ay_[IPT], az_[IPT];
+        float2 ax_[IPT], ay_[IPT], az_[IPT];
 #pragma unroll
-        for (int k = 0; k < IPT; ++k) ax_[k] = ay_[k] = az_[k] = 0.f;
-#pragma unroll 4
-        for (int jj = 0; jj < 32; ++jj) {
-            const float4 H = sh_hi[jj];
-            const float4 L = sh_lo[jj];
+        for (int k = 0; k < IPT; ++k) ax_[k] = ay_[k] = az_[k] = dup2(0.f);
+#pragma unroll 2
+        for (int p = 0; p < 16; ++p) {
+            const JPair jp = pair_tile_get(pt, p);
 #pragma unroll
             for (int k = 0; k < IPT; ++k)
-                pair_term<ZERO_SOFT>(H, L, xh[k], yh[k], zh[k], xl[k], yl[k], zl[k], eps2, ax_[k],
-                                     ay_[k], az_[k]);
+                pair_term2<ZERO_SOFT>(jp, nxh[k], nyh[k], nzh[k], nxl[k], nyl[k], nzl[k], e2,
+                                      ax_[k], ay_[k], az_[k]);
         }
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
-            kahan_add(sx[k], cx[k], ax_[k]);
-            kahan_add(sy[k], cy[k], ay_[k]);
-            kahan_add(sz[k], cz[k], az_[k]);
+            kahan_add(sx[k], cx[k], ax_[k].x + ax_[k].y);
+            kahan_add(sy[k], cy[k], ay_[k].x + ay_[k].y);
+            kahan_add(sz[k], cz[k], az_[k].x + az_[k].y);
         }
     }
 #pragma unroll
@@ -101,8 +102,7 @@ batch_force_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                    int num_items, int *__restrict__ counter, float eps2, double G,
                    double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az)
 {
-    __shared__ float4 sh_hi[kBatchWarps][32];
-    __shared__ float4 sh_lo[kBatchWarps][32];
+    __shared__ PairTile tiles[kBatchWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     while (true) {
         int item = 0;
@@ -113,16 +113,16 @@ batch_force_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
         const SysDesc sd = sys[w.sys];
         switch (sd.ipt) {
         case 1:
-            batch_item<1, ZERO_SOFT>(hi, lo, sd, w.i0, eps2, G, ax, ay, az, sh_hi[warp],
-                                     sh_lo[warp]);
+            batch_item<1, ZERO_SOFT>(hi, lo, sd, w.i0, eps2, G, ax, ay, az,
+                                     tiles[warp]);
             break;
         case 2:
-            batch_item<2, ZERO_SOFT>(hi, lo, sd, w.i0, eps2, G, ax, ay, az, sh_hi[warp],
-                                     sh_lo[warp]);
+            batch_item<2, ZERO_SOFT>(hi, lo, sd, w.i0, eps2, G, ax, ay, az,
+                                     tiles[warp]);
             break;
         default:
-            batch_item<4, ZERO_SOFT>(hi, lo, sd, w.i0, eps2, G, ax, ay, az, sh_hi[warp],
-                                     sh_lo[warp]);
+            batch_item<4, ZERO_SOFT>(hi, lo, sd, w.i0, eps2, G, ax, ay, az,
+                                     tiles[warp]);
             break;
         }
     }

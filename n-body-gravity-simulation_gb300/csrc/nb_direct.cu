@@ -11,10 +11,11 @@
 //    the pair is from the origin.  The rest of the pair term is plain FP32 on the
 //    FMA pipe with one MUFU rsqrt (rsqrt.approx.ftz.f32) whose ~1.3e-7 error is
 //    removed by a Newton step folded into r^-3 (3 extra FP32 ops: 21 FP32-pipe
-//    operations + 1 MUFU per pair against the 12 of the bare pair term).  Every
-//    thread owns
-//    IPT i-bodies, so one broadcast shared-memory read of a j-body feeds IPT pair
-//    terms.  Every 32 j the FP32 partial sum is added into a Kahan-compensated
+//    operations + 1 MUFU per pair against the 12 of the bare pair term).  The
+//    FP32 work runs as packed f32x2 operations on j-pairs (two j per
+//    instruction, nb_pair.cuh), which halves its issue slots.  Every thread
+//    owns IPT i-bodies, so one broadcast shared-memory read of a j-pair feeds
+//    IPT pair terms.  Every 32 j the FP32 partial sum is added into a Kahan-compensated
 //    (sum, compensation) pair; the CTA's partial over its j-segment is written
 //    as FP32 (sum, comp) and the segments are combined in FP64.
 //    The tensor cores stay idle: a softened 1/r^3 sum is not a contraction.
@@ -44,13 +45,13 @@ direct_mixed_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo
                     float eps2, int seg_len, float *__restrict__ psum,
                     float *__restrict__ pcomp)
 {
-    __shared__ float4 sh_hi[BLOCK];
-    __shared__ float4 sh_lo[BLOCK];
+    __shared__ PairTile tiles[BLOCK / 32];
 
     const int tid = threadIdx.x;
     const int ibase = blockIdx.x * (BLOCK * IPT);
 
-    float xh[IPT], yh[IPT], zh[IPT], xl[IPT], yl[IPT], zl[IPT];
+    // i-bodies negated and duplicated into f32x2 pairs
+    float2 nxh[IPT], nyh[IPT], nzh[IPT], nxl[IPT], nyl[IPT], nzl[IPT];
     float sx[IPT], sy[IPT], sz[IPT], cx[IPT], cy[IPT], cz[IPT];
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
@@ -60,11 +61,12 @@ direct_mixed_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo
             h = hi[i];
             l = lo[i];
         }
-        xh[k] = h.x; yh[k] = h.y; zh[k] = h.z;
-        xl[k] = l.x; yl[k] = l.y; zl[k] = l.z;
+        nxh[k] = dup2(-h.x); nyh[k] = dup2(-h.y); nzh[k] = dup2(-h.z);
+        nxl[k] = dup2(-l.x); nyl[k] = dup2(-l.y); nzl[k] = dup2(-l.z);
         sx[k] = sy[k] = sz[k] = 0.f;
         cx[k] = cy[k] = cz[k] = 0.f;
     }
+    const float2 e2 = dup2(eps2);
 
     const int j0 = blockIdx.y * seg_len;
     const int j1 = min(n, j0 + seg_len);
@@ -76,35 +78,32 @@ direct_mixed_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo
             l = lo[j];
         }
         __syncthreads();
-        sh_hi[tid] = h;
-        sh_lo[tid] = l;
+        pair_tile_put(tiles[tid >> 5], tid & 31, h.x, h.y, h.z, h.w, l.x, l.y, l.z);
         __syncthreads();
 
-        // FP32 partial sums over kSub consecutive j, Kahan-added into (s, c):
-        // the rounding of a running FP32 sum grows with its length, and 32
-        // terms keep it below the per-term error of the pair arithmetic.
-        constexpr int kSub = 32;
+        // FP32 partial sums over each 32-body tile (16 terms per f32x2 lane),
+        // Kahan-added into (s, c): the rounding of a running FP32 sum grows
+        // with its length, and short runs keep it below the per-term error of
+        // the pair arithmetic.
 #pragma unroll 1
-        for (int j0 = 0; j0 < BLOCK; j0 += kSub) {
-        float ax[IPT], ay[IPT], az[IPT];
+        for (int t = 0; t < BLOCK / 32; ++t) {
+            float2 ax[IPT], ay[IPT], az[IPT];
 #pragma unroll
-        for (int k = 0; k < IPT; ++k) ax[k] = ay[k] = az[k] = 0.f;
-
-#pragma unroll 4
-        for (int jj = j0; jj < j0 + kSub; ++jj) {
-            const float4 H = sh_hi[jj];
-            const float4 L = sh_lo[jj];
+            for (int k = 0; k < IPT; ++k) ax[k] = ay[k] = az[k] = dup2(0.f);
+#pragma unroll 2
+            for (int p = 0; p < 16; ++p) {
+                const JPair jp = pair_tile_get(tiles[t], p);
 #pragma unroll
-            for (int k = 0; k < IPT; ++k)
-                pair_term<ZERO_SOFT>(H, L, xh[k], yh[k], zh[k], xl[k], yl[k], zl[k], eps2,
-                                     ax[k], ay[k], az[k]);
-        }
+                for (int k = 0; k < IPT; ++k)
+                    pair_term2<ZERO_SOFT>(jp, nxh[k], nyh[k], nzh[k], nxl[k], nyl[k], nzl[k], e2,
+                                          ax[k], ay[k], az[k]);
+            }
 #pragma unroll
-        for (int k = 0; k < IPT; ++k) {
-            kahan_add(sx[k], cx[k], ax[k]);
-            kahan_add(sy[k], cy[k], ay[k]);
-            kahan_add(sz[k], cz[k], az[k]);
-        }
+            for (int k = 0; k < IPT; ++k) {
+                kahan_add(sx[k], cx[k], ax[k].x + ax[k].y);
+                kahan_add(sy[k], cy[k], ay[k].x + ay[k].y);
+                kahan_add(sz[k], cz[k], az[k].x + az[k].y);
+            }
         }
     }
 
@@ -278,7 +277,7 @@ constexpr int kF64Ipt = 2;
 struct MixShape {
     int block, ipt;
 };
-constexpr MixShape kMixShapes[] = {{256, 4}, {128, 8}, {128, 4}, {256, 2}, {64, 8}};
+constexpr MixShape kMixShapes[] = {{256, 4}, {128, 2}, {128, 4}, {256, 2}, {64, 4}};
 constexpr int kNumMixShapes = sizeof(kMixShapes) / sizeof(kMixShapes[0]);
 
 template <int B, int I>
@@ -292,10 +291,10 @@ int mix_slots()
 int mix_slots_for(int block, int ipt)
 {
     if (block == 256 && ipt == 4) return mix_slots<256, 4>();
-    if (block == 128 && ipt == 8) return mix_slots<128, 8>();
+    if (block == 128 && ipt == 2) return mix_slots<128, 2>();
     if (block == 128 && ipt == 4) return mix_slots<128, 4>();
     if (block == 256 && ipt == 2) return mix_slots<256, 2>();
-    if (block == 64 && ipt == 8) return mix_slots<64, 8>();
+    if (block == 64 && ipt == 4) return mix_slots<64, 4>();
     return 0;
 }
 
@@ -320,14 +319,14 @@ bool launch_mixed(const DirectPlan &p, cudaStream_t st, const float4 *hi, const 
     const int seg_len = p.seg_tiles * p.block;
     if (p.block == 256 && p.ipt == 4)
         launch_mixed_shape<256, 4>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
-    else if (p.block == 128 && p.ipt == 8)
-        launch_mixed_shape<128, 8>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
+    else if (p.block == 128 && p.ipt == 2)
+        launch_mixed_shape<128, 2>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
     else if (p.block == 128 && p.ipt == 4)
         launch_mixed_shape<128, 4>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
     else if (p.block == 256 && p.ipt == 2)
         launch_mixed_shape<256, 2>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
-    else if (p.block == 64 && p.ipt == 8)
-        launch_mixed_shape<64, 8>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
+    else if (p.block == 64 && p.ipt == 4)
+        launch_mixed_shape<64, 4>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
     else
         return false;
     return true;

@@ -28,8 +28,9 @@
 // Error of a far term: S carries one FP32 rounding of x - c.  With
 // |xi - c| <= D/2, |xj - c| <= r + D/2 and the subtraction's own rounding, the
 // displacement error is at most 2^-24 (2r + D) <= 2^-24 r (2 + 1/kFarFactor)
-// = 2^-22 r for kFarFactor = 1/2 -- about 2.4e-7 relative, the same order as
-// the FP32 arithmetic of the term.  Near terms keep the double-single
+// = 6 * 2^-24 r for kFarFactor = 1/4 -- about 3.6e-7 relative at worst, the
+// order of the FP32 arithmetic of the term (measured on a 65,536-body Plummer
+// sphere, factors 1/2, 1/4 and 1/8 leave the RMS force error at 3.2e-8).  Near terms keep the double-single
 // displacement (absolute error ~2^-48 |x|).  The folded Newton step on the
 // MUFU rsqrt is kept; every FP32 accumulator takes 32 terms before its
 // Kahan-compensated add, and the segments combine in FP64.
@@ -46,7 +47,7 @@ namespace nb {
 namespace {
 
 constexpr int kChunk = 32;             // j-chunk = one body per lane
-constexpr float kFarFactor2 = 0.25f;   // (gap / D)^2 threshold: kFarFactor = 1/2
+constexpr float kFarFactor2 = 0.0625f; // (gap / D)^2 threshold: kFarFactor = 1/4
 
 // Positions in Morton order relative to the root centre, split into
 // double-single hi/lo parts; mass in hi.w.
@@ -108,35 +109,6 @@ __device__ __forceinline__ void rel_ds(float h, float l, float c, float &S, floa
     two_sum(s, e + l, S, E);
 }
 
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
-
-// m r^-3 of a j-pair with the folded Newton step; ZERO_SOFT zeroes the
-// r2 == 0 (j == i) lane.
-template <bool ZERO_SOFT>
-__device__ __forceinline__ float2 pair_scale(float2 r2, float2 m)
-{
-    float2 inv = make_float2(rsqrt_mufu(r2.x), rsqrt_mufu(r2.y));
-    if (ZERO_SOFT) {
-        inv.x = r2.x > 0.f ? inv.x : 0.f;
-        inv.y = r2.y > 0.f ? inv.y : 0.f;
-    }
-    const float2 inv2 = mul2(inv, inv);
-    const float2 corr = fma2(dup2(-1.5f), mul2(r2, inv2), dup2(2.5f));
-    return mul2(mul2(mul2(m, inv), inv2), corr);
-}
-
-// One warp's staged j-chunk: j-pair p (bodies 2p and 2p+1 of the chunk) side
-// by side, so that one broadcast 16-byte load gives two f32x2 operands.
-struct ChunkStage {
-    float4 s[kChunk / 2];  // (Sx_2p, Sx_2p+1, Sy_2p, Sy_2p+1)
-    float4 t[kChunk / 2];  // (Sz_2p, Sz_2p+1, m_2p, m_2p+1)
-    float4 e[kChunk / 2];  // (Ex_2p, Ex_2p+1, Ey_2p, Ey_2p+1)
-    float2 f[kChunk / 2];  // (Ez_2p, Ez_2p+1)
-};
-
 // One warp = 32*IPT consecutive sorted i-bodies (chunks tile0 .. tile0+IPT-1,
 // lane l of chunk k holds body (tile0 + k) * 32 + l); blockIdx.y selects the
 // j-chunks [y * seg_chunks, (y + 1) * seg_chunks).  Writes per-segment Kahan
@@ -146,13 +118,14 @@ template <int WARPS, int IPT, bool ZERO_SOFT>
 __global__ void __launch_bounds__(WARPS * 32)
 direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                      const float4 *__restrict__ box, int n, int nchunks, float eps2,
-                     int seg_chunks, float *__restrict__ psum, float *__restrict__ pcomp)
+                     int seg_chunks, float *__restrict__ psum, float *__restrict__ pcomp,
+                     float far2)
 {
-    __shared__ ChunkStage stage[WARPS];
+    __shared__ PairTile stage[WARPS];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int tile0 = (blockIdx.x * WARPS + w) * IPT;
     if (tile0 >= nchunks) return;
-    ChunkStage &sg = stage[w];
+    PairTile &sg = stage[w];
 
     // the warp's box: union of its chunk boxes; centre and far threshold
     float bmn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, bmx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
@@ -165,9 +138,9 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
         }
     const float cx = 0.5f * (bmn[0] + bmx[0]), cy = 0.5f * (bmn[1] + bmx[1]),
                 cz = 0.5f * (bmn[2] + bmx[2]);
-    const float thr2 = kFarFactor2 * ((bmx[0] - bmn[0]) * (bmx[0] - bmn[0]) +
-                                      (bmx[1] - bmn[1]) * (bmx[1] - bmn[1]) +
-                                      (bmx[2] - bmn[2]) * (bmx[2] - bmn[2]));
+    const float thr2 = far2 * ((bmx[0] - bmn[0]) * (bmx[0] - bmn[0]) +
+                               (bmx[1] - bmn[1]) * (bmx[1] - bmn[1]) +
+                               (bmx[2] - bmn[2]) * (bmx[2] - bmn[2]));
 
     // i-bodies relative to c, negated and duplicated into pairs
     float2 nsx[IPT], nsy[IPT], nsz[IPT], nex[IPT], ney[IPT], nez[IPT];
@@ -207,10 +180,6 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
         l = lo[jc0 * kChunk + lane];
     }
     int pending = 0;  // chunks in the FP32 accumulators since the last Kahan add
-    float *const s_s = reinterpret_cast<float *>(&sg.s[lane >> 1]) + (lane & 1);
-    float *const s_t = reinterpret_cast<float *>(&sg.t[lane >> 1]) + (lane & 1);
-    float *const s_e = reinterpret_cast<float *>(&sg.e[lane >> 1]) + (lane & 1);
-    float *const s_f = reinterpret_cast<float *>(&sg.f[lane >> 1]) + (lane & 1);
     for (int jc = jc0; jc < jc1; ++jc) {
         const float4 jmn = box[2 * jc], jmx = box[2 * jc + 1];
         const float gx = fmaxf(0.f, fmaxf(jmn.x - bmx[0], bmn[0] - jmx.x));
@@ -228,13 +197,7 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
             mj = h.w;
         }
         __syncwarp();
-        s_s[0] = Sx;
-        s_s[2] = Sy;
-        s_t[0] = Sz;
-        s_t[2] = mj;
-        s_e[0] = Ex;
-        s_e[2] = Ey;
-        s_f[0] = Ez;
+        pair_tile_put(sg, lane, Sx, Sy, Sz, mj, Ex, Ey, Ez);
         __syncwarp();
         valid = jc + 1 < jc1 && (jc + 1) * kChunk + lane < n;
         if (valid) {
@@ -245,40 +208,19 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
         if (far) {
 #pragma unroll 4
             for (int p = 0; p < kChunk / 2; ++p) {
-                const float4 A = sg.s[p], B = sg.t[p];
-                const float2 X = make_float2(A.x, A.y), Y = make_float2(A.z, A.w);
-                const float2 Z = make_float2(B.x, B.y), M = make_float2(B.z, B.w);
+                const JPair j = pair_tile_get(sg, p);
 #pragma unroll
-                for (int k = 0; k < IPT; ++k) {
-                    const float2 dx = add2(X, nsx[k]);
-                    const float2 dy = add2(Y, nsy[k]);
-                    const float2 dz = add2(Z, nsz[k]);
-                    const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
-                    const float2 s = pair_scale<false>(r2, M);
-                    ax[k] = fma2(dx, s, ax[k]);
-                    ay[k] = fma2(dy, s, ay[k]);
-                    az[k] = fma2(dz, s, az[k]);
-                }
+                for (int k = 0; k < IPT; ++k)
+                    pair_term2_far(j, nsx[k], nsy[k], nsz[k], e2, ax[k], ay[k], az[k]);
             }
         } else {
 #pragma unroll 2
             for (int p = 0; p < kChunk / 2; ++p) {
-                const float4 A = sg.s[p], B = sg.t[p], C = sg.e[p];
-                const float2 F = sg.f[p];
-                const float2 X = make_float2(A.x, A.y), Y = make_float2(A.z, A.w);
-                const float2 Z = make_float2(B.x, B.y), M = make_float2(B.z, B.w);
-                const float2 EX = make_float2(C.x, C.y), EY = make_float2(C.z, C.w);
+                const JPair j = pair_tile_get(sg, p);
 #pragma unroll
-                for (int k = 0; k < IPT; ++k) {
-                    const float2 dx = add2(add2(X, nsx[k]), add2(EX, nex[k]));
-                    const float2 dy = add2(add2(Y, nsy[k]), add2(EY, ney[k]));
-                    const float2 dz = add2(add2(Z, nsz[k]), add2(F, nez[k]));
-                    const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
-                    const float2 s = pair_scale<ZERO_SOFT>(r2, M);
-                    ax[k] = fma2(dx, s, ax[k]);
-                    ay[k] = fma2(dy, s, ay[k]);
-                    az[k] = fma2(dz, s, az[k]);
-                }
+                for (int k = 0; k < IPT; ++k)
+                    pair_term2<ZERO_SOFT>(j, nsx[k], nsy[k], nsz[k], nex[k], ney[k], nez[k], e2,
+                                          ax[k], ay[k], az[k]);
             }
         }
         // every accumulator lane holds 16 terms per chunk: fold after two
@@ -369,10 +311,10 @@ void launch_sorted_shape(dim3 grid, cudaStream_t st, const float4 *hi, const flo
     const int nchunks = (n + kChunk - 1) / kChunk;
     if (eps2 > 0.0)
         direct_sorted_kernel<W, I, false><<<grid, W * 32, 0, st>>>(
-            hi, lo, box, n, nchunks, (float)eps2, seg_chunks, psum, pcomp);
+            hi, lo, box, n, nchunks, (float)eps2, seg_chunks, psum, pcomp, kFarFactor2);
     else
         direct_sorted_kernel<W, I, true><<<grid, W * 32, 0, st>>>(
-            hi, lo, box, n, nchunks, 0.0f, seg_chunks, psum, pcomp);
+            hi, lo, box, n, nchunks, 0.0f, seg_chunks, psum, pcomp, kFarFactor2);
 }
 
 // DirectPlan fields here: block = threads per CTA (32 * warps), ipt = chunks

@@ -96,7 +96,7 @@ struct SortedBuffers {
     void release();
 };
 // Bodies are sorted along a Morton curve; every warp re-centres the j-chunks
-// (32 bodies) that lie at least half its (compact) i-box diameter away on its
+// (32 bodies) that lie at least a quarter of its (compact) i-box diameter away on its
 // own box and runs the plain FP32 pair term on them; near chunks keep the
 // double-single one.
 nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,

@@ -56,4 +56,106 @@ __device__ __forceinline__ void pair_term(const float4 &H, const float4 &L, floa
     az = fmaf(dz, s, az);
 }
 
+// ---------------------------------------------------------------- packed f32x2
+// sm_100-class SMs run FP32 add, multiply and FMA on register pairs at the
+// FP32 pipe's lane rate for half the issue slots; each lane rounds exactly
+// like the scalar operation.  The packed kernels evaluate a j-pair (two
+// consecutive j of a 32-body tile) per operation against one i-body held as
+// negated, duplicated pairs.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+
+// m r^-3 of a j-pair with the folded Newton step of pair_term; ZERO_SOFT
+// zeroes the r2 == 0 (j == i) lane.
+template <bool ZERO_SOFT>
+__device__ __forceinline__ float2 pair_scale(float2 r2, float2 m)
+{
+    float2 inv = make_float2(rsqrt_mufu(r2.x), rsqrt_mufu(r2.y));
+    if (ZERO_SOFT) {
+        inv.x = r2.x > 0.f ? inv.x : 0.f;
+        inv.y = r2.y > 0.f ? inv.y : 0.f;
+    }
+    const float2 inv2 = mul2(inv, inv);
+    const float2 corr = fma2(dup2(-1.5f), mul2(r2, inv2), dup2(2.5f));
+    return mul2(mul2(mul2(m, inv), inv2), corr);
+}
+
+// A 32-body j-tile staged as 16 j-pairs side by side, so that one broadcast
+// 16-byte shared-memory load yields two f32x2 operands.  hi = (x, y, z, m),
+// lo = the double-single low parts (x, y, z).
+struct PairTile {
+    float4 s[16];  // (x_2p, x_2p+1, y_2p, y_2p+1)
+    float4 t[16];  // (z_2p, z_2p+1, m_2p, m_2p+1)
+    float4 e[16];  // (xlo_2p, xlo_2p+1, ylo_2p, ylo_2p+1)
+    float2 f[16];  // (zlo_2p, zlo_2p+1)
+};
+
+// Lane `lane` writes its j-body into the tile (call between two __syncwarp).
+__device__ __forceinline__ void pair_tile_put(PairTile &pt, int lane, float x, float y, float z,
+                                              float m, float xl, float yl, float zl)
+{
+    float *s = reinterpret_cast<float *>(&pt.s[lane >> 1]) + (lane & 1);
+    float *t = reinterpret_cast<float *>(&pt.t[lane >> 1]) + (lane & 1);
+    float *e = reinterpret_cast<float *>(&pt.e[lane >> 1]) + (lane & 1);
+    float *f = reinterpret_cast<float *>(&pt.f[lane >> 1]) + (lane & 1);
+    s[0] = x;
+    s[2] = y;
+    t[0] = z;
+    t[2] = m;
+    e[0] = xl;
+    e[2] = yl;
+    f[0] = zl;
+}
+
+// j-pair p of a tile as f32x2 operands.
+struct JPair {
+    float2 x, y, z, m, xl, yl, zl;
+};
+__device__ __forceinline__ JPair pair_tile_get(const PairTile &pt, int p)
+{
+    const float4 A = pt.s[p], B = pt.t[p], C = pt.e[p];
+    JPair j;
+    j.x = make_float2(A.x, A.y);
+    j.y = make_float2(A.z, A.w);
+    j.z = make_float2(B.x, B.y);
+    j.m = make_float2(B.z, B.w);
+    j.xl = make_float2(C.x, C.y);
+    j.yl = make_float2(C.z, C.w);
+    j.zl = pt.f[p];
+    return j;
+}
+
+// The double-single pair term of pair_term for a j-pair against one i-body
+// given as negated duplicated pairs (nxh = (-xh, -xh), ...).
+template <bool ZERO_SOFT>
+__device__ __forceinline__ void pair_term2(const JPair &j, float2 nxh, float2 nyh, float2 nzh,
+                                           float2 nxl, float2 nyl, float2 nzl, float2 e2,
+                                           float2 &ax, float2 &ay, float2 &az)
+{
+    const float2 dx = add2(add2(j.x, nxh), add2(j.xl, nxl));
+    const float2 dy = add2(add2(j.y, nyh), add2(j.yl, nyl));
+    const float2 dz = add2(add2(j.z, nzh), add2(j.zl, nzl));
+    const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+    const float2 s = pair_scale<ZERO_SOFT>(r2, j.m);
+    ax = fma2(dx, s, ax);
+    ay = fma2(dy, s, ay);
+    az = fma2(dz, s, az);
+}
+
+// The plain FP32 term (coordinates already relative to a nearby origin).
+__device__ __forceinline__ void pair_term2_far(const JPair &j, float2 nx, float2 ny, float2 nz,
+                                               float2 e2, float2 &ax, float2 &ay, float2 &az)
+{
+    const float2 dx = add2(j.x, nx);
+    const float2 dy = add2(j.y, ny);
+    const float2 dz = add2(j.z, nz);
+    const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+    const float2 s = pair_scale<false>(r2, j.m);
+    ax = fma2(dx, s, ax);
+    ay = fma2(dy, s, ay);
+    az = fma2(dz, s, az);
+}
+
 } // namespace nb
