@@ -191,6 +191,53 @@ def cpu_reference_rate(n, target_seconds, threads=0):
     return x, y, z, m, rows, cores, O
 
 
+def pair_abs_sums(st, torch, tile=2048):
+    """S_i = sum_j m_j |r_j - r_i| / (|r_j - r_i|^2 + eps^2)^(3/2) in FP64 on
+    the GPU (torch), the error scale of any FP32 evaluation of a_i."""
+    import numpy as np
+    p = torch.from_numpy(np.stack([st["x"], st["y"], st["z"]], 1)).cuda()
+    m = torch.from_numpy(np.ascontiguousarray(st["m"])).cuda()
+    out = torch.empty(p.shape[0], dtype=torch.float64, device="cuda")
+    for i0 in range(0, p.shape[0], tile):
+        d = p[None, :, :] - p[i0:i0 + tile, None, :]
+        r2 = (d * d).sum(-1)
+        t = m[None, :] * torch.sqrt(r2) / (r2 + EPS * EPS) ** 1.5
+        out[i0:i0 + tile] = t.sum(1)
+        del d, r2, t
+    return out.cpu().numpy()
+
+
+def reference_gpu_kernel_rate(st, n, inter, mixed_rate, torch, stream):
+    """The reference's own FP64 GPU kernel (computeAccelerationNaiveKernel,
+    compiled for sm_103a from its source into oracle/_ref) on the same bodies,
+    launched as ForceCalculatorNaive does; CUDA events around two launches."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import ref_gpu
+    if not ref_gpu.available():
+        return {"unavailable": "reference cubin not built (no reference sources here)"}
+    k = ref_gpu.RefNaiveKernel()
+    dev = [torch.from_numpy(np.ascontiguousarray(st[c])).cuda() for c in ("x", "y", "z", "m")]
+    acc = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    ptrs = [t.data_ptr() for t in dev[:3] + acc] + [dev[3].data_ptr()]
+    torch.cuda.synchronize()
+    k.launch(*ptrs, n, EPS * EPS, stream=stream.cuda_stream)  # warm
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 2
+    e0.record(stream)
+    for _ in range(reps):
+        k.launch(*ptrs, n, EPS * EPS, stream=stream.cuda_stream)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    k.close()
+    rate = inter / (ms / 1e3) / 1e9
+    return {"value": rate, "unit": UNIT, "kind": "reference",
+            "kernel": "computeAccelerationNaiveKernel (CUDA/src/force_calculator_naive.cu:4-59),"
+                      " sm_103a cubin, ceil(N/256) x 256 threads",
+            "kernel_ms": ms, "mixed_kernel_speedup": mixed_rate / rate}
+
+
 # ---------------------------------------------------------------- reference arm
 def run_reference(a, rank, world):
     if rank != 0:
@@ -443,7 +490,9 @@ def run_ours(a, rank, world, local_rank):
     clk = clocks.summary(t_wall0, t_wall1)
     peak = fp32_roofline_gint(props.multi_processor_count, peaks.get("sm_max_mhz", 2070.0))
     roofline = {
-        "bound": "fp32", "kernel": "direct_mixed_kernel", "achieved": achieved,
+        "bound": "fp32",
+        "kernel": "direct_sorted_kernel" if n >= 8192 else "direct_mixed_kernel",
+        "achieved": achieved,
         "peak": peak, "unit": "Ginteractions/s", "frac": achieved / peak,
         "peak_basis": (f"{props.multi_processor_count} SMs x {peaks.get('sm_max_mhz', 2070.0)}"
                        f" MHz ({peak_kind} sm_max_mhz) x 128 FP32 lanes / 12 FP32 ops per "
@@ -454,7 +503,7 @@ def run_ours(a, rank, world, local_rank):
     if clk.get("sm_mhz"):
         roofline["frac_at_measured_clock"] = achieved / fp32_roofline_gint(
             props.multi_processor_count, clk["sm_mhz"])
-    roofline["traffic"] = profiled_traffic("direct_mixed_n65536.md") if n == N_BODIES else None
+    roofline["traffic"] = profiled_traffic("direct_sorted_n65536.md") if n == N_BODIES else None
     roofline["algorithmic_bytes"] = 32 * n  # hi + lo mirror of every body, read once
 
     extras = {}
@@ -485,12 +534,23 @@ def run_ours(a, rank, world, local_rank):
         r = np.sqrt(sum(v * v for v in ref_acc))
         rel = d / np.maximum(r, 1e-300)
         fp64_rate = inter / (p64["force_kernel_ms"] / 1e3) / 1e9
-        extras["force_error_vs_fp64"] = {"max_rel": float(rel.max()),
-                                         "rms_rel": float(np.sqrt(np.mean(rel * rel))),
-                                         "max_abs_over_rms_a": float(d.max() /
-                                                                     np.sqrt(np.mean(r * r)))}
+        sabs = pair_abs_sums(st, torch)
+        kappa = sabs / np.maximum(r, 1e-300)
+        well = kappa <= 10.0
+        extras["force_error_vs_fp64"] = {
+            "max_rel": float(rel.max()),
+            "rms_rel": float(np.sqrt(np.mean(rel * rel))),
+            "max_abs_over_rms_a": float(d.max() / np.sqrt(np.mean(r * r))),
+            "max_rel_kappa_le_10": float(rel[well].max(initial=0.0)),
+            "max_err_over_abs_sum": float((d / np.maximum(sabs, 1e-300)).max()),
+            "kappa_at_max_rel": float(kappa[rel.argmax()]),
+            "bodies_kappa_gt_10": int((~well).sum()),
+            "note": ("kappa = sum_j |pair term| / |a|: a body whose force nearly cancels "
+                     "(large kappa) carries a relative error ~kappa x that of its terms")}
         extras["fp64_direct"] = {"gint_s": fp64_rate, "kernel": "direct_fp64_kernel",
                                  "mixed_speedup": achieved / fp64_rate}
+        extras["gpu_baseline"] = reference_gpu_kernel_rate(st, n, inter, achieved, torch,
+                                                           stream)
 
     if not a.skip_extras and rank == 0 and a.bh_steps > 0:
         extras["barnes_hut"] = run_bh(a, nb, torch, dev, stream, flush, np)

@@ -17,7 +17,8 @@
 //    owns IPT i-bodies, so one broadcast shared-memory read of a j-pair feeds
 //    IPT pair terms.  Every 32 j the FP32 partial sum is added into a Kahan-compensated
 //    (sum, compensation) pair; the CTA's partial over its j-segment is written
-//    as FP32 (sum, comp) and the segments are combined in FP64.
+//    as FP32 (sum, comp) and the segments are combined as a double-single,
+//    scaled by G in FP64.
 //    The tensor cores stay idle: a softened 1/r^3 sum is not a contraction.
 //
 //  * direct_fp64_kernel -- the 1e-12 path: the same tiling in FP64.
@@ -123,7 +124,8 @@ direct_mixed_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo
     }
 }
 
-// a_i = G * sum_s (sum_s - comp_s), in FP64, segments in index order.
+// a_i = G * sum_s (sum_s - comp_s), segments in index order, accumulated as a
+// double-single and scaled in FP64.
 __global__ void combine_mixed_kernel(const float *__restrict__ psum,
                                      const float *__restrict__ pcomp, int n, int segments,
                                      double G, double *__restrict__ ax,
@@ -132,16 +134,16 @@ __global__ void combine_mixed_kernel(const float *__restrict__ psum,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const size_t plane = (size_t)n;
-    double a[3] = {0.0, 0.0, 0.0};
+    float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
     for (int s = 0; s < segments; ++s) {
         const size_t base = (size_t)s * 3 * plane;
 #pragma unroll
         for (int c = 0; c < 3; ++c)
-            a[c] += (double)psum[base + c * plane + i] - (double)pcomp[base + c * plane + i];
+            ds_add_kahan(hi[c], lo[c], psum[base + c * plane + i], pcomp[base + c * plane + i]);
     }
-    ax[i] = G * a[0];
-    ay[i] = G * a[1];
-    az[i] = G * a[2];
+    ax[i] = G * ((double)hi[0] + (double)lo[0]);
+    ay[i] = G * ((double)hi[1] + (double)lo[1]);
+    az[i] = G * ((double)hi[2] + (double)lo[2]);
 }
 
 template <int BLOCK, int IPT, bool ZERO_SOFT>

@@ -33,7 +33,7 @@
 // sphere, factors 1/2, 1/4 and 1/8 leave the RMS force error at 3.2e-8).  Near terms keep the double-single
 // displacement (absolute error ~2^-48 |x|).  The folded Newton step on the
 // MUFU rsqrt is kept; every FP32 accumulator takes 32 terms before its
-// Kahan-compensated add, and the segments combine in FP64.
+// Kahan-compensated add, and the segments combine as a double-single.
 #include "nb_internal.h"
 #include "nb_pair.cuh"
 
@@ -48,6 +48,7 @@ namespace {
 
 constexpr int kChunk = 32;             // j-chunk = one body per lane
 constexpr float kFarFactor2 = 0.0625f; // (gap / D)^2 threshold: kFarFactor = 1/4
+constexpr int kResortEvals = 8;        // force evaluations per Morton re-sort
 
 // Positions in Morton order relative to the root centre, split into
 // double-single hi/lo parts; mass in hi.w.
@@ -252,7 +253,8 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
     }
 }
 
-// a[order[i]] = G * sum_s (sum_s - comp_s) for sorted body i, in FP64.
+// a[order[i]] = G * sum_s (sum_s - comp_s) for sorted body i: a double-single
+// sum over the segments, scaled in FP64.
 __global__ void combine_sorted_kernel(const float *__restrict__ psum,
                                       const float *__restrict__ pcomp, int n, int segments,
                                       double G, const uint32_t *__restrict__ order,
@@ -262,17 +264,17 @@ __global__ void combine_sorted_kernel(const float *__restrict__ psum,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const size_t plane = (size_t)n;
-    double a[3] = {0.0, 0.0, 0.0};
+    float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
     for (int s = 0; s < segments; ++s) {
         const size_t base = (size_t)s * 3 * plane;
 #pragma unroll
         for (int c = 0; c < 3; ++c)
-            a[c] += (double)psum[base + c * plane + i] - (double)pcomp[base + c * plane + i];
+            ds_add_kahan(hi[c], lo[c], psum[base + c * plane + i], pcomp[base + c * plane + i]);
     }
     const uint32_t o = order[i];
-    ax[o] = G * a[0];
-    ay[o] = G * a[1];
-    az[o] = G * a[2];
+    ax[o] = G * ((double)hi[0] + (double)lo[0]);
+    ay[o] = G * ((double)hi[1] + (double)lo[1]);
+    az[o] = G * ((double)hi[2] + (double)lo[2]);
 }
 
 struct SortedShape {
@@ -368,6 +370,9 @@ void SortedBuffers::release()
     boxes.release();
     if (sorter) bh_destroy(sorter);
     sorter = nullptr;
+    order = nullptr;
+    centre = nullptr;
+    order_n = -1;
 }
 
 bool direct_sorted_enabled(int n)
@@ -399,12 +404,20 @@ static nb_status autotune_sorted(const float4 *hi, const float4 *lo, int n, doub
     NB_CUDA_TRY(cudaEventCreate(&e0));
     NB_CUDA_TRY(cudaEventCreate(&e1));
     float best_ms = 1e30f;
+    // Above 2^18 bodies every shape is timed on all i-bodies against the first
+    // 512 j-chunks only (one segment): an evaluation there takes 0.1 s and more.
+    const bool probe = n > (1 << 18);
     for (int k = 0; k < kNumSortedShapes; ++k) {
         const DirectPlan p = sorted_plan_for_shape(n, kSortedShapes[k].warps, kSortedShapes[k].ipt);
+        DirectPlan t = p;
+        if (probe) {
+            t.segments = 1;
+            t.seg_tiles = std::min(p.seg_tiles * p.segments, 512);
+        }
         float *psum = nullptr;
-        NB_TRY(run_sorted(p, hi, lo, n, eps2, b, st, &psum));
+        NB_TRY(run_sorted(t, hi, lo, n, eps2, b, st, &psum));
         cudaEventRecord(e0, st);
-        for (int r = 0; r < 2; ++r) NB_TRY(run_sorted(p, hi, lo, n, eps2, b, st, &psum));
+        for (int r = 0; r < 2; ++r) NB_TRY(run_sorted(t, hi, lo, n, eps2, b, st, &psum));
         cudaEventRecord(e1, st);
         NB_CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0.f;
@@ -427,10 +440,15 @@ nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
 {
     if (n <= 0) return NB_OK;
     if (!b.sorter) b.sorter = bh_create();
-    const uint32_t *order = nullptr;
-    const double *centre = nullptr;
-    // 10 levels of the Morton curve: cells far smaller than a 32-body chunk
-    NB_TRY(bh_morton_order(b.sorter, x, y, z, n, 10, st, &order, &centre));
+    if (b.order_n != n || b.evals_since_sort >= kResortEvals) {
+        // 10 levels of the Morton curve: cells far smaller than a 32-body chunk
+        NB_TRY(bh_morton_order(b.sorter, x, y, z, n, 10, st, &b.order, &b.centre));
+        b.order_n = n;
+        b.evals_since_sort = 0;
+    }
+    ++b.evals_since_sort;
+    const uint32_t *order = b.order;
+    const double *centre = b.centre;
     const int nchunks = (n + kChunk - 1) / kChunk;
     NB_TRY(b.hi.reserve(sizeof(float4) * (size_t)n));
     NB_TRY(b.lo.reserve(sizeof(float4) * (size_t)n));

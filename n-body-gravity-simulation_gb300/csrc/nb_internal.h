@@ -93,6 +93,14 @@ struct BHTree;
 struct SortedBuffers {
     DevBuf hi, lo, partials, boxes;
     BHTree *sorter = nullptr;
+    // The Morton order is a performance device only (near/far decisions use
+    // the current chunk boxes), so it is recomputed every kResortEvals force
+    // evaluations, when n changes and after every load, not at every call.
+    const uint32_t *order = nullptr;  // sorted index -> body (sorter-owned)
+    const double *centre = nullptr;   // origin of the hi/lo split (sorter-owned)
+    int order_n = -1;
+    int evals_since_sort = 0;
+    void invalidate_order() { order_n = -1; }
     void release();
 };
 // Bodies are sorted along a Morton curve; every warp re-centres the j-chunks

@@ -1,5 +1,6 @@
 // nb_pair.cuh -- the mixed-precision pair term shared by the all-pairs kernels
-// (single system, nb_direct.cu) and the batched ensemble (nb_ensemble.cu).
+// (nb_direct.cu, nb_direct_sorted.cu) and the batched work-queue kernel
+// (nb_batch.cu).
 //
 // A body is a float4 hi = (x, y, z, m) and a float4 lo = (x - hi, y - hi,
 // z - hi, 0): a double-single copy of its FP64 position.  The displacement
@@ -30,6 +31,20 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float t)
     float u = s + y;
     c = (u - s) - y;
     s = u;
+}
+
+// (hi, lo) += s - c: a segment's Kahan pair (sum s, compensation c) added
+// into a double-single accumulator with FP32 operations (two-sum of hi and s;
+// the rounding error and -c go to lo).  The FP64 pipe of a GB300 SM runs at a
+// small fraction of its FP32 rate, so partial sums are combined this way and
+// converted to FP64 once: (double)hi + (double)lo.
+__device__ __forceinline__ void ds_add_kahan(float &hi, float &lo, float s, float c)
+{
+    const float t = hi + s;
+    const float bb = t - hi;
+    const float e = (hi - (t - bb)) + (s - bb);
+    hi = t;
+    lo = lo + (e - c);
 }
 
 // a += m_j (r_j - r_i) / (|r_j - r_i|^2 + eps2)^(3/2) for one (i, j) pair.

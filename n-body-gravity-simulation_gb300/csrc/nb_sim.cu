@@ -312,6 +312,7 @@ static nb_status load_impl(nb_sim *s, size_t n, const double *const *src, cudaMe
         NB_CUDA_TRY(cudaMemsetAsync(s->f[k], 0, bytes, s->stream));
     s->n = n;
     s->forces_valid = false;
+    s->sorted.invalidate_order();
     return NB_OK;
 }
 
@@ -362,7 +363,10 @@ nb_status nb_bind_device(nb_sim *s, size_t n, double *const *arrays10)
         s->f[k] = arrays10[k];
     }
     s->n = n;
-    if (!same) s->forces_valid = false;
+    if (!same) {
+        s->forces_valid = false;
+        s->sorted.invalidate_order();
+    }
     return NB_OK;
 }
 

@@ -36,3 +36,16 @@ REF_SOURCES=(
     -I"$REF_ROOT/CPU/include" -o "$HERE/_ref/libnbref.so.tmp" \
     "$HERE/ref_shim.cpp" "${REF_SOURCES[@]}"
 mv -f "$HERE/_ref/libnbref.so.tmp" "$HERE/_ref/libnbref.so"
+
+# The reference's FP64 GPU kernel (computeAccelerationNaiveKernel,
+# CUDA/src/force_calculator_naive.cu:4-59) as a standalone sm_103a cubin, compiled
+# where it lies with the reference Makefile's flags (-std=c++17 -O3) and the
+# architecture switched to sm_103a.  Device code only: it carries no host code,
+# so it runs on any host of the GPU machine; ref_gpu.py loads it with the driver API.
+CUDA_SRC="$REF_ROOT/CUDA/src/force_calculator_naive.cu"
+NVCC="${NVCC:-$(command -v nvcc || echo /usr/local/cuda/bin/nvcc)}"
+if [[ -f "$CUDA_SRC" && -x "$NVCC" ]]; then
+    "$NVCC" -std=c++17 -O3 -cubin -gencode arch=compute_103a,code=sm_103a \
+        -I"$REF_ROOT/CUDA/include" -o "$HERE/_ref/ref_naive_sm103a.cubin.tmp" "$CUDA_SRC"
+    mv -f "$HERE/_ref/ref_naive_sm103a.cubin.tmp" "$HERE/_ref/ref_naive_sm103a.cubin"
+fi
