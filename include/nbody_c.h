@@ -41,7 +41,8 @@ typedef enum nb_status {
     NB_ERR_CAPACITY = 4,     /* more bodies than the object was created for */
     NB_ERR_NOT_LOADED = 5,   /* no bodies loaded yet */
     NB_ERR_DEVICE_FAULT = 6, /* a kernel reported an error status */
-    NB_ERR_UNSUPPORTED = 7
+    NB_ERR_UNSUPPORTED = 7,
+    NB_ERR_IO = 8            /* a file could not be opened, read, parsed or written */
 } nb_status;
 
 /* Force methods.
@@ -320,6 +321,51 @@ nb_status nb_gen_disk_bulge(size_t n, uint64_t seed, double total_mass, double b
                             double bulge_scale, double disk_scale, double disk_height,
                             double dispersion, double G, double *x, double *y, double *z,
                             double *vx, double *vy, double *vz, double *m);
+
+/* ---- files: particle lists, trajectory CSV, checkpoints (host side) ---------- */
+
+/* Reads the reference's particle file, the format its test loader parses
+ * (CUDA/tests/test3_correctness.cu:16-38, fixtures particles_{100..10000}.txt):
+ * the body count N, then N records "m x y z vx vy vz", whitespace-separated.
+ * With m == NULL only *n is set (a size query).  Otherwise every array must
+ * hold `capacity` >= N doubles.  Errors: NB_ERR_IO (missing or malformed
+ * file), NB_ERR_CAPACITY. */
+nb_status nb_particles_read(const char *path, size_t capacity, size_t *n, double *m, double *x,
+                            double *y, double *z, double *vx, double *vy, double *vz);
+/* Writes the same format, 17 significant digits (reads back bit-exactly). */
+nb_status nb_particles_write(const char *path, size_t n, const double *m, const double *x,
+                             const double *y, const double *z, const double *vx,
+                             const double *vy, const double *vz);
+/* nb_particles_read into the simulation (nb_load of the file's bodies). */
+nb_status nb_load_particles(nb_sim *sim, const char *path);
+
+/* Appends one row of the reference's trajectory CSV (CPU/src/n-body.cpp:6-58,
+ * CPU/orbit.csv): the x y z of each listed body, then kinetic, potential
+ * (unsoftened) and total energy, angular momentum x y z and centre of mass
+ * x y z of the simulation's current state (nb_diagnostics).  header != 0
+ * first writes the header line: "<name>_x,<name>_y,<name>_z" per listed body,
+ * then kinetic_energy,...,center_of_mass_z.  precision < 0 prints numbers as a
+ * default C++ stream does (6 significant digits, %g); precision >= 0 prints
+ * them fixed with that many decimals (the reference writes its first row the
+ * first way and every later row with 15).  The file is created if missing. */
+nb_status nb_csv_append(nb_sim *sim, const char *path, int nbodies, const int *bodies,
+                        const char *const *names, int header, int precision);
+
+/* Binary checkpoint of a simulation: configuration, body count, whether the
+ * stored accelerations are those of the stored positions (leapfrog and
+ * velocity Verlet then continue without a new force evaluation, as the
+ * reference's integrators do after their first step), and the ten FP64
+ * planes x y z vx vy vz ax ay az m.  Layout: 8-byte magic "NBGB3CK1", uint32
+ * version 1, uint32 forces_valid, uint64 n, nb_config, then the planes
+ * (native byte order).  No reference counterpart (the reference keeps no
+ * state on disk). */
+nb_status nb_checkpoint_save(nb_sim *sim, const char *path);
+/* Restores configuration, state and the accelerations flag; n must fit the
+ * simulation's capacity.  Continuing after a restore gives the same bits as
+ * continuing the saved run for the FP64 and Barnes-Hut methods and for the
+ * mixed method below 8192 bodies; above, the mixed path re-sorts the bodies on
+ * load, which changes its summation order (results stay within tolerance). */
+nb_status nb_checkpoint_load(nb_sim *sim, const char *path);
 
 /* ---- all-pairs forces without device allocation ----------------------------- */
 

@@ -500,6 +500,7 @@ const char *nb_status_string(nb_status s)
     case NB_ERR_NOT_LOADED: return "no bodies loaded";
     case NB_ERR_DEVICE_FAULT: return "device-reported error";
     case NB_ERR_UNSUPPORTED: return "unsupported";
+    case NB_ERR_IO: return "file input/output error";
     }
     return "unknown status";
 }

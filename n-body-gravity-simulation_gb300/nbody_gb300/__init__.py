@@ -31,7 +31,7 @@ EULER, EULER_CROMER, LEAPFROG, VELOCITY_VERLET, RK4 = 0, 1, 2, 3, 4
 
 STATUS = {0: "NB_OK", 1: "NB_ERR_INVALID_ARGUMENT", 2: "NB_ERR_CUDA", 3: "NB_ERR_OUT_OF_MEMORY",
           4: "NB_ERR_CAPACITY", 5: "NB_ERR_NOT_LOADED", 6: "NB_ERR_DEVICE_FAULT",
-          7: "NB_ERR_UNSUPPORTED"}
+          7: "NB_ERR_UNSUPPORTED", 8: "NB_ERR_IO"}
 
 # Every function declared in include/nbody_c.h (checked by the tests).
 EXPORTS = [
@@ -43,6 +43,8 @@ EXPORTS = [
     "nb_gen_plummer", "nb_gen_disk_bulge", "nb_status_string", "nb_last_error", "nb_version",
     "nb_profile_enable", "nb_profile_read", "nb_kernel_launch_count",
     "nb_direct_mixed_forces_noalloc",
+    "nb_particles_read", "nb_particles_write", "nb_load_particles", "nb_csv_append",
+    "nb_checkpoint_save", "nb_checkpoint_load",
     "nb_ensemble_create", "nb_ensemble_destroy", "nb_ensemble_load", "nb_ensemble_read_state",
     "nb_ensemble_compute_forces", "nb_ensemble_step", "nb_ensemble_tune",
     "nb_ensemble_synchronize", "nb_ensemble_info", "nb_ensemble_profile",
@@ -174,6 +176,12 @@ def lib():
     L.nb_kernel_launch_count.restype = C.c_uint64
     L.nb_direct_mixed_forces_noalloc.argtypes = ([sz] + [vp] * 4 + [C.c_double] * 2 +
                                                  [vp] * 3 + [vp])
+    L.nb_particles_read.argtypes = [C.c_char_p, sz, C.POINTER(sz)] + [vp] * 7
+    L.nb_particles_write.argtypes = [C.c_char_p, sz] + [vp] * 7
+    L.nb_load_particles.argtypes = [vp, C.c_char_p]
+    L.nb_csv_append.argtypes = [vp, C.c_char_p, C.c_int, vp, vp, C.c_int, C.c_int]
+    L.nb_checkpoint_save.argtypes = [vp, C.c_char_p]
+    L.nb_checkpoint_load.argtypes = [vp, C.c_char_p]
     L.nb_ensemble_create.argtypes = [C.POINTER(_Config), C.c_int, vp, vp, C.POINTER(vp)]
     L.nb_ensemble_destroy.argtypes = [vp]
     L.nb_ensemble_load.argtypes = [vp] + [vp] * 7
@@ -235,6 +243,25 @@ def disk_bulge(n: int, seed: int = 0, total_mass: float = 1.0, bulge_frac: float
                                    disk_height, dispersion, G, *map(_ptr, out)),
            "nb_gen_disk_bulge")
     return tuple(out)
+
+
+def read_particles(path: str):
+    """The reference's particle file (N, then "m x y z vx vy vz" per body);
+    returns (x, y, z, vx, vy, vz, m) as float64 arrays."""
+    n = C.c_size_t()
+    bp = os.fsencode(path)
+    _check(lib().nb_particles_read(bp, 0, C.byref(n), *([None] * 7)), "nb_particles_read")
+    cols = [np.empty(n.value) for _ in range(7)]  # m x y z vx vy vz
+    _check(lib().nb_particles_read(bp, n.value, C.byref(n), *map(_ptr, cols)),
+           "nb_particles_read")
+    m, x, y, z, vx, vy, vz = cols
+    return x, y, z, vx, vy, vz, m
+
+
+def write_particles(path: str, x, y, z, vx, vy, vz, m):
+    cols = [_f64(v) for v in (m, x, y, z, vx, vy, vz)]
+    _check(lib().nb_particles_write(os.fsencode(path), len(cols[0]), *map(_ptr, cols)),
+           "nb_particles_write")
 
 
 # ------------------------------------------------------------------ simulation
@@ -354,6 +381,28 @@ class Sim:
         _check(lib().nb_profile_read(self._h, C.byref(p), int(reset)), "nb_profile_read")
         return dict(kernel_launches=p.kernel_launches, force_launches=p.force_launches,
                     force_kernel_ms=p.force_kernel_ms)
+
+    # -------------------------------------------------------------- files
+    def load_particles(self, path: str):
+        _check(lib().nb_load_particles(self._h, os.fsencode(path)), "nb_load_particles")
+
+    def csv_append(self, path: str, bodies, names=None, header: bool = False,
+                   precision: int = 15):
+        """One trajectory-CSV row (positions of `bodies`, energies, L, COM)."""
+        idx = np.ascontiguousarray(bodies, dtype=np.int32)
+        arr = None
+        if names is not None:
+            enc = [os.fsencode(str(v)) for v in names]
+            arr = (C.c_char_p * len(enc))(*enc)
+        _check(lib().nb_csv_append(self._h, os.fsencode(path), len(idx), _ptr(idx),
+                                   C.cast(arr, C.c_void_p) if arr is not None else None,
+                                   int(header), precision), "nb_csv_append")
+
+    def checkpoint_save(self, path: str):
+        _check(lib().nb_checkpoint_save(self._h, os.fsencode(path)), "nb_checkpoint_save")
+
+    def checkpoint_load(self, path: str):
+        _check(lib().nb_checkpoint_load(self._h, os.fsencode(path)), "nb_checkpoint_load")
 
     # -------------------------------------------------------------- Barnes-Hut
     def bh_build(self) -> dict:
