@@ -316,6 +316,8 @@ def run_bh(a, nb, torch, dev, stream, flush, np):
            "steps": a.bh_steps, "ms_per_step": ms, "steps_per_s": 1e3 / ms,
            "walk_ms": walk_ms, "walk_share": walk_ms / ms,
            "interactions_per_body": inter / n,
+           "m2p_per_body": info["interactions_m2p"] / n,
+           "p2p_per_body": info["interactions_p2p"] / n,
            "walk_ginteractions_s": inter / (walk_ms / 1e3) / 1e9,
            "nodes": info["num_nodes"], "leaves": info["num_leaves"],
            "max_depth": info["max_depth"], "timing": "CUDA events per leapfrog step, L2 "

@@ -40,6 +40,7 @@
 // num_nodes steps: there is no stack to overflow.  Accelerations are scattered
 // back to the original order in FP64, multiplied by G.
 #include "nb_internal.h"
+#include "nb_pair.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -68,12 +69,13 @@ struct BHRoot {
     int pad;
 };
 
+// A leaf is the node whose skip pointer is the next node (no subtree).
 struct alignas(32) BHNode {
     float4 com_mass;  // centre of mass relative to the root centre, mass
     int first;        // first sorted body
     int count;        // bodies in the cell
     int skip;         // next node (preorder) outside this subtree
-    int meta;         // depth | leaf << 8
+    float size2;      // squared side of the cell (the opening test's size^2)
 };
 static_assert(sizeof(BHNode) == 32, "node layout");
 
@@ -530,7 +532,8 @@ __global__ void __launch_bounds__(256)
 node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__restrict__ root,
             const int *__restrict__ chain_len, const int *__restrict__ chain_depth,
             const int *__restrict__ offsets, const D4 *__restrict__ P,
-            BHNode *__restrict__ nodes, BHStats *__restrict__ stats)
+            BHNode *__restrict__ nodes, unsigned char *__restrict__ node_depth,
+            BHStats *__restrict__ stats)
 {
     const int i = blockIdx.x * 256 + threadIdx.x;
     if (i >= n) return;
@@ -555,8 +558,9 @@ node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__rest
         nd.first = i;
         nd.count = cnt;
         nd.skip = offsets[i + cnt];
-        nd.meta = d | (leaf ? 256 : 0);
+        nd.size2 = root->size2[d];
         nodes[id0 + k] = nd;
+        node_depth[id0 + k] = (unsigned char)d;
         leaves += leaf;
         maxd = max(maxd, d);
     }
@@ -565,54 +569,65 @@ node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__rest
 }
 
 // ------------------------------------------------------------ walk
-__device__ __forceinline__ float rsqrt_approx(float x)
-{
-    float r;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
 constexpr int kWalkBlock = 128;
 
+// ZERO_SOFT: eps2 == 0, where the lane's own body (r2 == 0) contributes 0.
+template <bool ZERO_SOFT>
 __global__ void __launch_bounds__(kWalkBlock)
 walk_kernel(const BHNode *__restrict__ nodes, int num_nodes, const float4 *__restrict__ body,
-            const uint32_t *__restrict__ order, int n, const BHRoot *__restrict__ root,
-            float theta2, float eps2, double G, double *__restrict__ ax,
-            double *__restrict__ ay, double *__restrict__ az, BHStats *__restrict__ stats)
+            const uint32_t *__restrict__ order, int n, float theta2, float eps2, double G,
+            double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
+            BHStats *__restrict__ stats)
 {
-    __shared__ float size2[kMaxLevels + 1];
-    if (threadIdx.x <= kMaxLevels) size2[threadIdx.x] = root->size2[threadIdx.x];
-    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int warp0 = (blockIdx.x * kWalkBlock + threadIdx.x) - lane;
     if (warp0 >= n) return;  // whole warp past the end
     const int i = warp0 + lane;
     const bool valid = i < n;
     const float4 p = body[valid ? i : n - 1];
-    float fx = 0.f, fy = 0.f, fz = 0.f;
+    const float2 npx = dup2(-p.x), npy = dup2(-p.y), npz = dup2(-p.z), e2 = dup2(eps2);
+    float fx = 0.f, fy = 0.f, fz = 0.f;                         // monopoles, odd bodies
+    float2 gx = dup2(0.f), gy = dup2(0.f), gz = dup2(0.f);     // leaf bodies in pairs
     unsigned m2p = 0, p2p = 0;
     int node = 0;
     while (node < num_nodes) {
         const BHNode nd = nodes[node];
-        const int depth = nd.meta & 255;
-        const bool leaf = (nd.meta >> 8) != 0;
         const float dx = nd.com_mass.x - p.x;
         const float dy = nd.com_mass.y - p.y;
         const float dz = nd.com_mass.z - p.z;
         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const bool mine = (unsigned)(i - nd.first) < (unsigned)nd.count;
-        const bool open = valid && (mine || size2[depth] >= theta2 * d2);
+        const bool open = valid && (mine || nd.size2 >= theta2 * d2);
         if (__any_sync(0xffffffffu, open)) {
-            if (!leaf) {
+            if (nd.skip != node + 1) {  // internal: descend
                 ++node;
                 continue;
             }
+            // leaf: its bodies, two per f32x2 instruction
             const int e = nd.first + nd.count;
-            for (int b = nd.first; b < e; ++b) {
+            int b = nd.first;
+            for (; b + 1 < e; b += 2) {
+                const float4 q0 = body[b], q1 = body[b + 1];
+                const float2 rx = add2(make_float2(q0.x, q1.x), npx);
+                const float2 ry = add2(make_float2(q0.y, q1.y), npy);
+                const float2 rz = add2(make_float2(q0.z, q1.z), npz);
+                const float2 r2 = fma2(rz, rz, fma2(ry, ry, fma2(rx, rx, e2)));
+                float2 inv = make_float2(rsqrt_mufu(r2.x), rsqrt_mufu(r2.y));
+                if (ZERO_SOFT) {
+                    inv.x = r2.x > 0.f ? inv.x : 0.f;
+                    inv.y = r2.y > 0.f ? inv.y : 0.f;
+                }
+                const float2 s = mul2(mul2(make_float2(q0.w, q1.w), inv), mul2(inv, inv));
+                gx = fma2(rx, s, gx);
+                gy = fma2(ry, s, gy);
+                gz = fma2(rz, s, gz);
+            }
+            if (b < e) {
                 const float4 q = body[b];
                 const float rx = q.x - p.x, ry = q.y - p.y, rz = q.z - p.z;
                 const float r2 = fmaf(rz, rz, fmaf(ry, ry, fmaf(rx, rx, eps2)));
-                const float inv = r2 > 0.f ? rsqrt_approx(r2) : 0.f;  // the self term
+                float inv = rsqrt_mufu(r2);
+                if (ZERO_SOFT) inv = r2 > 0.f ? inv : 0.f;
                 const float s = (q.w * inv) * (inv * inv);
                 fx = fmaf(rx, s, fx);
                 fy = fmaf(ry, s, fy);
@@ -620,7 +635,7 @@ walk_kernel(const BHNode *__restrict__ nodes, int num_nodes, const float4 *__res
             }
             p2p += nd.count;
         } else {
-            const float inv = rsqrt_approx(d2 + eps2);
+            const float inv = rsqrt_mufu(d2 + eps2);
             const float s = (nd.com_mass.w * inv) * (inv * inv);
             fx = fmaf(dx, s, fx);
             fy = fmaf(dy, s, fy);
@@ -631,9 +646,9 @@ walk_kernel(const BHNode *__restrict__ nodes, int num_nodes, const float4 *__res
     }
     if (valid) {
         const uint32_t o = order[i];
-        ax[o] = G * (double)fx;
-        ay[o] = G * (double)fy;
-        az[o] = G * (double)fz;
+        ax[o] = G * ((double)fx + ((double)gx.x + (double)gx.y));
+        ay[o] = G * ((double)fy + ((double)gy.x + (double)gy.y));
+        az[o] = G * ((double)fz + ((double)gz.x + (double)gz.y));
     }
     // every lane ran the same interactions: count once per valid lane
     const unsigned nv = __popc(__ballot_sync(0xffffffffu, valid));
@@ -666,7 +681,7 @@ struct BHTree {
     int n = 0;
     int num_nodes = 0;
     DevBuf part, root, keys0, keys1, vals0, vals1, hist, body, moments, prefix, chain_len,
-        chain_depth, offsets, scan_tmp, nodes, stats;
+        chain_depth, offsets, scan_tmp, nodes, node_depth, stats;
     const uint64_t *sorted_codes = nullptr;
     const uint32_t *order = nullptr;
 };
@@ -678,7 +693,8 @@ void bh_destroy(BHTree *t)
     if (!t) return;
     DevBuf *bufs[] = {&t->part, &t->root, &t->keys0, &t->keys1, &t->vals0, &t->vals1,
                       &t->hist, &t->body, &t->moments, &t->prefix, &t->chain_len,
-                      &t->chain_depth, &t->offsets, &t->scan_tmp, &t->nodes, &t->stats};
+                      &t->chain_depth, &t->offsets, &t->scan_tmp, &t->nodes, &t->node_depth,
+                      &t->stats};
     for (DevBuf *b : bufs) b->release();
     delete t;
 }
@@ -780,20 +796,30 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     NB_CUDA_TRY(cudaStreamSynchronize(st));
     if (total <= 0) return fail(NB_ERR_DEVICE_FAULT, "Barnes-Hut: empty tree");
     if ((size_t)total * sizeof(BHNode) > t->nodes.bytes)
-        NB_TRY(t->nodes.reserve(sizeof(BHNode) * ((size_t)total + total / 4 + 1024)));
+    {
+        const size_t room = (size_t)total + total / 4 + 1024;
+        NB_TRY(t->nodes.reserve(sizeof(BHNode) * room));
+        NB_TRY(t->node_depth.reserve(room));
+    }
     t->num_nodes = total;
     t->n = n;
     NB_CUDA_TRY(cudaMemsetAsync(stats, 0, sizeof(BHStats), st));
     node_kernel<<<div_up(n, 256), 256, 0, st>>>(kin, n, leaf_capacity, root,
                                                 t->chain_len.as<int>(), t->chain_depth.as<int>(),
                                                 t->offsets.as<int>(), t->prefix.as<D4>(),
-                                                t->nodes.as<BHNode>(), stats);
+                                                t->nodes.as<BHNode>(),
+                                                t->node_depth.as<unsigned char>(), stats);
     NB_LAUNCH_CHECK();
     if (!ax) return NB_OK;
     if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
-    walk_kernel<<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
-        t->nodes.as<BHNode>(), total, t->body.as<float4>(), vin, n, root,
-        (float)(theta * theta), (float)eps2, G, ax, ay, az, stats);
+    if (eps2 > 0.0)
+        walk_kernel<false><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
+            t->nodes.as<BHNode>(), total, t->body.as<float4>(), vin, n, (float)(theta * theta),
+            (float)eps2, G, ax, ay, az, stats);
+    else
+        walk_kernel<true><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
+            t->nodes.as<BHNode>(), total, t->body.as<float4>(), vin, n, (float)(theta * theta),
+            0.0f, G, ax, ay, az, stats);
     NB_LAUNCH_CHECK();
     if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
     return NB_OK;
@@ -841,9 +867,12 @@ nb_status bh_read_nodes(BHTree *t, cudaStream_t st, int max_nodes, int *depth,
     if (max_nodes < t->num_nodes)
         return fail(NB_ERR_CAPACITY, "max_nodes is smaller than the node count");
     std::vector<BHNode> h(t->num_nodes);
+    std::vector<unsigned char> dep(t->num_nodes);
     std::vector<uint64_t> codes(t->n);
     BHRoot r;
     NB_CUDA_TRY(cudaMemcpyAsync(h.data(), t->nodes.ptr, sizeof(BHNode) * h.size(),
+                                cudaMemcpyDeviceToHost, st));
+    NB_CUDA_TRY(cudaMemcpyAsync(dep.data(), t->node_depth.ptr, dep.size(),
                                 cudaMemcpyDeviceToHost, st));
     NB_CUDA_TRY(cudaMemcpyAsync(codes.data(), t->sorted_codes, sizeof(uint64_t) * t->n,
                                 cudaMemcpyDeviceToHost, st));
@@ -851,12 +880,12 @@ nb_status bh_read_nodes(BHTree *t, cudaStream_t st, int max_nodes, int *depth,
     NB_CUDA_TRY(cudaStreamSynchronize(st));
     for (int k = 0; k < t->num_nodes; ++k) {
         const BHNode &nd = h[k];
-        const int d = nd.meta & 255;
+        const int d = dep[k];
         if (depth) depth[k] = d;
         if (prefix) prefix[k] = d == 0 ? 0 : codes[nd.first] >> (63 - 3 * d);
         if (first) first[k] = nd.first;
         if (count) count[k] = nd.count;
-        if (is_leaf) is_leaf[k] = (nd.meta >> 8) != 0;
+        if (is_leaf) is_leaf[k] = nd.skip == k + 1;
         if (skip) skip[k] = nd.skip;
         if (com_mass) {
             com_mass[4 * k + 0] = (float)(r.cx + (double)nd.com_mass.x);
