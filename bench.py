@@ -286,58 +286,72 @@ def run_bh(a, nb, torch, dev, stream, flush, np):
     FP32 walk / FP64 integration, leapfrog dt = 1e-3.  Reports steps/s over
     a.bh_steps leapfrog steps (CUDA events per step, L2 flushed before each),
     the walk kernel's share and rate, and the force error against the mixed
-    direct sum on a sample of bodies."""
+    direct sum; then the same with the tree rebuilt every 4 evaluations and
+    refitted in between (NB_FLAG_BH_REUSE(4))."""
     n = a.bh_n
     state = nb.disk_bulge(n, seed=SEED)
-    cfg = nb.Config(method=nb.BARNES_HUT, G=1.0, softening=EPS, theta=BH_THETA, leaf_capacity=8)
-    sim = nb.Sim(cfg, capacity=n, stream=stream.cuda_stream)
-    sim.load(*state)
-    for _ in range(3):
-        sim.step(nb.LEAPFROG, BH_DT, 1)
-    torch.cuda.synchronize()
-    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(a.bh_steps)]
-    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(a.bh_steps)]
-    sim.profile(True)
-    sim.profile_read(reset=True)
-    for k in range(a.bh_steps):
-        flush.zero_()
-        ev0[k].record(stream)
-        sim.step(nb.LEAPFROG, BH_DT, 1)
-        ev1[k].record(stream)
-    torch.cuda.synchronize()
-    prof = sim.profile_read(reset=True)
-    sim.profile(False)
-    step_ms = [e0.elapsed_time(e1) for e0, e1 in zip(ev0, ev1)]
-    info = sim.bh_info()
-    inter = info["interactions_m2p"] + info["interactions_p2p"]
-    walk_ms = prof["force_kernel_ms"] / max(1, prof["force_launches"])
-    ms = sum(step_ms) / len(step_ms)
+
+    def timed(flags):
+        cfg = nb.Config(method=nb.BARNES_HUT, G=1.0, softening=EPS, theta=BH_THETA,
+                        leaf_capacity=8, flags=flags)
+        sim = nb.Sim(cfg, capacity=n, stream=stream.cuda_stream)
+        sim.load(*state)
+        for _ in range(3):
+            sim.step(nb.LEAPFROG, BH_DT, 1)
+        torch.cuda.synchronize()
+        ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(a.bh_steps)]
+        ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(a.bh_steps)]
+        sim.profile(True)
+        sim.profile_read(reset=True)
+        for k in range(a.bh_steps):
+            flush.zero_()
+            ev0[k].record(stream)
+            sim.step(nb.LEAPFROG, BH_DT, 1)
+            ev1[k].record(stream)
+        torch.cuda.synchronize()
+        prof = sim.profile_read(reset=True)
+        sim.profile(False)
+        step_ms = [e0.elapsed_time(e1) for e0, e1 in zip(ev0, ev1)]
+        info = sim.bh_info()
+        inter = info["interactions_m2p"] + info["interactions_p2p"]
+        walk_ms = prof["force_kernel_ms"] / max(1, prof["force_launches"])
+        ms = sum(step_ms) / len(step_ms)
+        out = {"ms_per_step": ms, "steps_per_s": 1e3 / ms,
+               "walk_ms": walk_ms, "walk_share": walk_ms / ms,
+               "interactions_per_body": inter / n,
+               "m2p_per_body": info["interactions_m2p"] / n,
+               "p2p_per_body": info["interactions_p2p"] / n,
+               "walk_ginteractions_s": inter / (walk_ms / 1e3) / 1e9,
+               "nodes": info["num_nodes"], "leaves": info["num_leaves"],
+               "max_depth": info["max_depth"]}
+        # accuracy of the last evaluation vs the mixed direct sum (itself
+        # within ~1e-6 of FP64)
+        st = sim.read_state()
+        bh_acc = (st["ax"], st["ay"], st["az"])
+        ref = nb.Sim(nb.Config(method=nb.DIRECT_MIXED, G=1.0, softening=EPS), capacity=n,
+                     stream=stream.cuda_stream)
+        ref.load(st["x"], st["y"], st["z"], st["vx"], st["vy"], st["vz"], st["m"])
+        ref.compute_forces()
+        ra = ref.accelerations()
+        ref.close()
+        sim.close()
+        d = np.sqrt(sum((u - v) ** 2 for u, v in zip(bh_acc, ra)))
+        r = np.sqrt(sum(v * v for v in ra))
+        rel = d / np.maximum(r, 1e-300)
+        out["force_error_vs_direct"] = {"mean_rel": float(rel.mean()),
+                                        "max_rel": float(rel.max()),
+                                        "p99_rel": float(np.quantile(rel, 0.99))}
+        return out
+
     out = {"workload": f"disk_bulge_n{n}_theta{BH_THETA}_leapfrog", "n": n,
-           "steps": a.bh_steps, "ms_per_step": ms, "steps_per_s": 1e3 / ms,
-           "walk_ms": walk_ms, "walk_share": walk_ms / ms,
-           "interactions_per_body": inter / n,
-           "m2p_per_body": info["interactions_m2p"] / n,
-           "p2p_per_body": info["interactions_p2p"] / n,
-           "walk_ginteractions_s": inter / (walk_ms / 1e3) / 1e9,
-           "nodes": info["num_nodes"], "leaves": info["num_leaves"],
-           "max_depth": info["max_depth"], "timing": "CUDA events per leapfrog step, L2 "
-                                                     "flushed before each; includes one host "
-                                                     "read of the node count per step"}
-    # accuracy vs the mixed direct sum (itself within ~1e-6 of FP64)
-    st = sim.read_state()
-    bh_acc = (st["ax"], st["ay"], st["az"])
-    ref = nb.Sim(nb.Config(method=nb.DIRECT_MIXED, G=1.0, softening=EPS), capacity=n,
-                 stream=stream.cuda_stream)
-    ref.load(st["x"], st["y"], st["z"], st["vx"], st["vy"], st["vz"], st["m"])
-    ref.compute_forces()
-    ra = ref.accelerations()
-    ref.close()
-    d = np.sqrt(sum((u - v) ** 2 for u, v in zip(bh_acc, ra)))
-    r = np.sqrt(sum(v * v for v in ra))
-    rel = d / np.maximum(r, 1e-300)
-    out["force_error_vs_direct"] = {"mean_rel": float(rel.mean()), "max_rel": float(rel.max()),
-                                    "p99_rel": float(np.quantile(rel, 0.99))}
-    sim.close()
+           "steps": a.bh_steps}
+    out.update(timed(0))
+    out["timing"] = ("CUDA events per leapfrog step, L2 flushed before each; a build reads "
+                     "the node count on the host once per step")
+    reuse = timed(nb.bh_reuse_flag(4))
+    out["tree_reuse_4"] = {k: reuse[k] for k in ("ms_per_step", "steps_per_s", "walk_ms",
+                                                 "interactions_per_body",
+                                                 "force_error_vs_direct")}
     return out
 
 

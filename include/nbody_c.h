@@ -80,9 +80,19 @@ typedef struct nb_config {
 
 /* flags */
 #define NB_FLAG_NONE 0
-/* Report the reference's unsoftened potential energy as `potential` (default:
- * both are always reported, see nb_diag). */
+/* Bit 0 is reserved. */
 #define NB_FLAG_RESERVED 1
+/* Barnes-Hut tree reuse (bits 8-15): NB_FLAG_BH_REUSE(k), k >= 2, rebuilds the
+ * tree every k force evaluations; the evaluations in between keep the last
+ * build's topology and body order and refit monopoles and cell sides to the
+ * current positions (a cell's side becomes the larger of its cube side and its
+ * bodies' bounding-box extent, so a drifted cell opens at least as readily as
+ * a rebuilt one).  k = 0 or 1 (the default) rebuilds at every evaluation, as
+ * BarnesHutForceCalculator::computeAccelerations does
+ * (CUDA/src/force_calculator_barnes_hut.cu:625-671).  A load, a configuration
+ * change or a checkpoint restore forces a rebuild. */
+#define NB_FLAG_BH_REUSE(k) (((k) & 0xff) << 8)
+#define NB_FLAG_BH_REUSE_OF(flags) (((flags) >> 8) & 0xff)
 
 typedef struct nb_sim nb_sim;
 

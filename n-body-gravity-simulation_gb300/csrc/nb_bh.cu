@@ -568,6 +568,71 @@ node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__rest
     atomicMax(&stats->max_depth, maxd);
 }
 
+// ------------------------------------------------------------ refit
+// Tree reuse: the topology and body order of the last build are kept while
+// the bodies move; every evaluation in between recomputes the monopoles from
+// the bodies' current positions and replaces each cell's side by the larger of
+// its cube side and the extent of its bodies' bounding box, so a drifted cell
+// is opened at least as readily as a freshly built one would be.
+__device__ __forceinline__ float box_ext2(float4 lo, float4 hi)
+{
+    const float e = fmaxf(hi.x - lo.x, fmaxf(hi.y - lo.y, hi.z - lo.z));
+    return e * e;
+}
+
+// Monopoles of every node; bounding boxes and sides of the leaves.
+__global__ void __launch_bounds__(256)
+refit_kernel(BHNode *__restrict__ nodes, int num_nodes,
+             const unsigned char *__restrict__ node_depth, const D4 *__restrict__ P,
+             const BHRoot *__restrict__ root, const float4 *__restrict__ body,
+             float4 *__restrict__ boxes)
+{
+    const int k = blockIdx.x * 256 + threadIdx.x;
+    if (k >= num_nodes) return;
+    BHNode nd = nodes[k];
+    const D4 hi = P[nd.first + nd.count], lo = P[nd.first];
+    const double mass = hi.x - lo.x;
+    nd.com_mass = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (mass > 0.0)
+        nd.com_mass = make_float4((float)((hi.y - lo.y) / mass), (float)((hi.z - lo.z) / mass),
+                                  (float)((hi.w - lo.w) / mass), (float)mass);
+    if (nd.skip == k + 1) {  // leaf
+        float4 mn = body[nd.first], mx = mn;
+        for (int b = nd.first + 1; b < nd.first + nd.count; ++b) {
+            const float4 q = body[b];
+            mn = make_float4(fminf(mn.x, q.x), fminf(mn.y, q.y), fminf(mn.z, q.z), 0.f);
+            mx = make_float4(fmaxf(mx.x, q.x), fmaxf(mx.y, q.y), fmaxf(mx.z, q.z), 0.f);
+        }
+        boxes[2 * k] = mn;
+        boxes[2 * k + 1] = mx;
+        nd.size2 = fmaxf(root->size2[node_depth[k]], box_ext2(mn, mx));
+    }
+    nodes[k] = nd;
+}
+
+// Internal nodes of depth d: box = union of the children's boxes (children:
+// node + 1, then each child's skip pointer up to the node's own).
+__global__ void __launch_bounds__(256)
+refit_level_kernel(BHNode *__restrict__ nodes, int num_nodes,
+                   const unsigned char *__restrict__ node_depth, int d,
+                   const BHRoot *__restrict__ root, float4 *__restrict__ boxes)
+{
+    const int k = blockIdx.x * 256 + threadIdx.x;
+    if (k >= num_nodes || node_depth[k] != d) return;
+    const int skip = nodes[k].skip;
+    if (skip == k + 1) return;  // leaf: done by refit_kernel
+    float4 mn = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f);
+    float4 mx = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
+    for (int c = k + 1; c < skip; c = nodes[c].skip) {
+        const float4 a = boxes[2 * c], b = boxes[2 * c + 1];
+        mn = make_float4(fminf(mn.x, a.x), fminf(mn.y, a.y), fminf(mn.z, a.z), 0.f);
+        mx = make_float4(fmaxf(mx.x, b.x), fmaxf(mx.y, b.y), fmaxf(mx.z, b.z), 0.f);
+    }
+    boxes[2 * k] = mn;
+    boxes[2 * k + 1] = mx;
+    nodes[k].size2 = fmaxf(root->size2[d], box_ext2(mn, mx));
+}
+
 // ------------------------------------------------------------ walk
 constexpr int kWalkBlock = 128;
 
@@ -681,10 +746,17 @@ struct BHTree {
     int n = 0;
     int num_nodes = 0;
     DevBuf part, root, keys0, keys1, vals0, vals1, hist, body, moments, prefix, chain_len,
-        chain_depth, offsets, scan_tmp, nodes, node_depth, stats;
+        chain_depth, offsets, scan_tmp, nodes, node_depth, boxes, stats;
     const uint64_t *sorted_codes = nullptr;
     const uint32_t *order = nullptr;
+    bool tree_valid = false;    // nodes/order describe a build of these bodies' count
+    int evals_since_build = 0;  // walks on the current topology
 };
+
+void bh_invalidate(BHTree *t)
+{
+    if (t) t->tree_valid = false;
+}
 
 BHTree *bh_create() { return new BHTree(); }
 
@@ -694,7 +766,7 @@ void bh_destroy(BHTree *t)
     DevBuf *bufs[] = {&t->part, &t->root, &t->keys0, &t->keys1, &t->vals0, &t->vals1,
                       &t->hist, &t->body, &t->moments, &t->prefix, &t->chain_len,
                       &t->chain_depth, &t->offsets, &t->scan_tmp, &t->nodes, &t->node_depth,
-                      &t->stats};
+                      &t->boxes, &t->stats};
     for (DevBuf *b : bufs) b->release();
     delete t;
 }
@@ -760,12 +832,66 @@ nb_status bh_morton_order(BHTree *t, const double *x, const double *y, const dou
     return NB_OK;
 }
 
+static nb_status launch_walk(BHTree *t, int n, double G, double eps2, double theta, double *ax,
+                             double *ay, double *az, cudaStream_t st, const KernelTimer *timer)
+{
+    BHStats *stats = t->stats.as<BHStats>();
+    const uint32_t *order = t->order;
+    if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
+    if (eps2 > 0.0)
+        walk_kernel<false><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
+            t->nodes.as<BHNode>(), t->num_nodes, t->body.as<float4>(), order, n,
+            (float)(theta * theta), (float)eps2, G, ax, ay, az, stats);
+    else
+        walk_kernel<true><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
+            t->nodes.as<BHNode>(), t->num_nodes, t->body.as<float4>(), order, n,
+            (float)(theta * theta), 0.0f, G, ax, ay, az, stats);
+    NB_LAUNCH_CHECK();
+    if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
+    return NB_OK;
+}
+
+// Monopoles and cell sides of the kept topology for the current positions.
+static nb_status refit(BHTree *t, const double *x, const double *y, const double *z,
+                       const double *m, int n, cudaStream_t st)
+{
+    const BHRoot *root = t->root.as<BHRoot>();
+    const int nn = t->num_nodes;
+    NB_TRY(t->boxes.reserve(sizeof(float4) * 2 * (size_t)nn));
+    gather_kernel<<<div_up(n, 256), 256, 0, st>>>(t->order, x, y, z, m, n, root,
+                                                  t->body.as<float4>(), t->moments.as<D4>());
+    NB_LAUNCH_CHECK();
+    NB_TRY(scan_exclusive<D4>(t->moments.as<D4>(), n, t->prefix.as<D4>(), t->scan_tmp, st));
+    refit_kernel<<<div_up(nn, 256), 256, 0, st>>>(t->nodes.as<BHNode>(), nn,
+                                                  t->node_depth.as<unsigned char>(),
+                                                  t->prefix.as<D4>(), root, t->body.as<float4>(),
+                                                  t->boxes.as<float4>());
+    NB_LAUNCH_CHECK();
+    // internal nodes, deepest first (an internal node is shallower than the
+    // deepest possible level)
+    for (int d = kMaxLevels - 1; d >= 0; --d) {
+        refit_level_kernel<<<div_up(nn, 256), 256, 0, st>>>(
+            t->nodes.as<BHNode>(), nn, t->node_depth.as<unsigned char>(), d, root,
+            t->boxes.as<float4>());
+        NB_LAUNCH_CHECK();
+    }
+    // this walk's interaction counts (the tree's leaf and depth figures stay)
+    NB_CUDA_TRY(cudaMemsetAsync(t->stats.ptr, 0, 2 * sizeof(unsigned long long), st));
+    return NB_OK;
+}
+
 nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *z,
                      const double *m, int n, double G, double eps2, double theta,
                      int leaf_capacity, double *ax, double *ay, double *az, cudaStream_t st,
-                     const KernelTimer *timer)
+                     const KernelTimer *timer, int reuse)
 {
     if (n <= 0) return NB_OK;
+    if (ax && reuse > 1 && t->tree_valid && t->n == n && t->evals_since_build < reuse) {
+        NB_TRY(refit(t, x, y, z, m, n, st));
+        ++t->evals_since_build;
+        return launch_walk(t, n, G, eps2, theta, ax, ay, az, st, timer);
+    }
+    t->tree_valid = false;
     const size_t N = (size_t)n;
     NB_TRY(t->body.reserve(sizeof(float4) * N));
     NB_TRY(t->moments.reserve(sizeof(D4) * N));
@@ -795,8 +921,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
                                 cudaMemcpyDeviceToHost, st));
     NB_CUDA_TRY(cudaStreamSynchronize(st));
     if (total <= 0) return fail(NB_ERR_DEVICE_FAULT, "Barnes-Hut: empty tree");
-    if ((size_t)total * sizeof(BHNode) > t->nodes.bytes)
-    {
+    if ((size_t)total * sizeof(BHNode) > t->nodes.bytes) {
         const size_t room = (size_t)total + total / 4 + 1024;
         NB_TRY(t->nodes.reserve(sizeof(BHNode) * room));
         NB_TRY(t->node_depth.reserve(room));
@@ -810,19 +935,11 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
                                                 t->nodes.as<BHNode>(),
                                                 t->node_depth.as<unsigned char>(), stats);
     NB_LAUNCH_CHECK();
+    t->tree_valid = true;
+    t->evals_since_build = 0;
     if (!ax) return NB_OK;
-    if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
-    if (eps2 > 0.0)
-        walk_kernel<false><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
-            t->nodes.as<BHNode>(), total, t->body.as<float4>(), vin, n, (float)(theta * theta),
-            (float)eps2, G, ax, ay, az, stats);
-    else
-        walk_kernel<true><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
-            t->nodes.as<BHNode>(), total, t->body.as<float4>(), vin, n, (float)(theta * theta),
-            0.0f, G, ax, ay, az, stats);
-    NB_LAUNCH_CHECK();
-    if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
-    return NB_OK;
+    t->evals_since_build = 1;
+    return launch_walk(t, n, G, eps2, theta, ax, ay, az, st, timer);
 }
 
 nb_status bh_info(BHTree *t, cudaStream_t st, nb_bh_info *info)

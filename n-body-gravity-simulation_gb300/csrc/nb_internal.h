@@ -187,11 +187,15 @@ struct BHTree;  // opaque, defined in nb_bh.cu
 BHTree *bh_create();
 void bh_destroy(BHTree *t);
 // Builds the tree of (x,y,z,m) and, when ax != nullptr, walks it writing
-// G * acceleration (FP64) in the original body order.
+// G * acceleration (FP64) in the original body order.  reuse > 1: the tree is
+// rebuilt every `reuse` walks; the walks in between keep its topology and
+// refit monopoles and cell sides to the current positions.
 nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *z,
                      const double *m, int n, double G, double eps2, double theta,
                      int leaf_capacity, double *ax, double *ay, double *az, cudaStream_t st,
-                     const KernelTimer *timer = nullptr);
+                     const KernelTimer *timer = nullptr, int reuse = 1);
+// The next bh_compute rebuilds (the bodies were replaced).
+void bh_invalidate(BHTree *t);
 nb_status bh_info(BHTree *t, cudaStream_t st, nb_bh_info *info);
 // Morton order of the bodies by the top 3*levels code bits: *order maps a
 // sorted index to the original one; *root_centre points at the device copy of

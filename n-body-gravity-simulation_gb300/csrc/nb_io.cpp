@@ -255,6 +255,7 @@ nb_status nb_checkpoint_load(nb_sim *s, const char *path)
     s->n = n;
     s->forces_valid = valid != 0;
     s->sorted.invalidate_order();
+    nb::bh_invalidate(s->bh);
     return NB_OK;
 }
 

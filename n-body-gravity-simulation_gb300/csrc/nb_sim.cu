@@ -120,7 +120,8 @@ nb_status eval_forces(nb_sim *s, const double *px, const double *py, const doubl
     case NB_BARNES_HUT:
         if (!s->bh) s->bh = bh_create();
         return bh_compute(s->bh, px, py, pz, s->m(), n, s->cfg.G, eps2, s->cfg.theta,
-                          s->cfg.leaf_capacity, oax, oay, oaz, s->stream, timer);
+                          s->cfg.leaf_capacity, oax, oay, oaz, s->stream, timer,
+                          NB_FLAG_BH_REUSE_OF(s->cfg.flags));
     default:
         return fail(NB_ERR_INVALID_ARGUMENT, "unknown force method");
     }
@@ -286,7 +287,10 @@ nb_status nb_set_config(nb_sim *s, const nb_config *cfg)
                       s->cfg.softening == cfg->softening && s->cfg.theta == cfg->theta &&
                       s->cfg.leaf_capacity == cfg->leaf_capacity;
     s->cfg = *cfg;
-    if (!same) s->forces_valid = false;
+    if (!same) {
+        s->forces_valid = false;
+        bh_invalidate(s->bh);
+    }
     return NB_OK;
 }
 
@@ -313,6 +317,7 @@ static nb_status load_impl(nb_sim *s, size_t n, const double *const *src, cudaMe
     s->n = n;
     s->forces_valid = false;
     s->sorted.invalidate_order();
+    bh_invalidate(s->bh);
     return NB_OK;
 }
 
@@ -366,6 +371,7 @@ nb_status nb_bind_device(nb_sim *s, size_t n, double *const *arrays10)
     if (!same) {
         s->forces_valid = false;
         s->sorted.invalidate_order();
+        bh_invalidate(s->bh);
     }
     return NB_OK;
 }

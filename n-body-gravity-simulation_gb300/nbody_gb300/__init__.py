@@ -113,6 +113,11 @@ def kernel_launch_count() -> int:
     return int(lib().nb_kernel_launch_count())
 
 
+def bh_reuse_flag(k: int) -> int:
+    """NB_FLAG_BH_REUSE(k): rebuild the Barnes-Hut tree every k evaluations."""
+    return (int(k) & 0xFF) << 8
+
+
 @dataclass
 class Config:
     method: int = DIRECT_MIXED

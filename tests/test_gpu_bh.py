@@ -246,3 +246,60 @@ def test_leapfrog_energy(nb):
         s.step(nb.LEAPFROG, 1e-3, 50)
         e1 = s.diagnostics()["total_softened"]
     assert abs(e1 - e0) / abs(e0) < 1e-4
+
+
+def test_tree_reuse_keeps_accuracy(nb):
+    """NB_FLAG_BH_REUSE(4): three of every four evaluations refit the last
+    tree.  Against the FP64 direct sum of the same positions, every refit
+    evaluation is as accurate as a rebuilt one (the drifted cells' sides grow
+    with their bounding boxes), and the interaction count stays close."""
+    n, dt = 20000, 2e-3
+    st = nb.disk_bulge(n, seed=21)
+
+    def run(flags):
+        errs, inter = [], []
+        cfg = nb.Config(method=nb.BARNES_HUT, G=1.0, softening=1e-3, theta=0.5, flags=flags)
+        with nb.Sim(cfg, capacity=n) as s, \
+                nb.Sim(nb.Config(method=nb.DIRECT_FP64, G=1.0, softening=1e-3),
+                       capacity=n) as ref:
+            s.load(*st)
+            for _ in range(8):
+                s.step(nb.LEAPFROG, dt)
+                cur = s.read_state()
+                info = s.bh_info()
+                inter.append(info["interactions_m2p"] + info["interactions_p2p"])
+                ref.load(cur["x"], cur["y"], cur["z"], cur["vx"], cur["vy"], cur["vz"],
+                         cur["m"])
+                ref.compute_forces()
+                a_ref = ref.accelerations()
+                d = np.sqrt(sum((cur[k] - v) ** 2 for k, v in zip(("ax", "ay", "az"), a_ref)))
+                r = np.sqrt(sum(v * v for v in a_ref))
+                errs.append(float(np.mean(d / r)))
+        return np.array(errs), np.array(inter, dtype=float)
+
+    e1, i1 = run(0)
+    e4, i4 = run(nb.bh_reuse_flag(4))
+    assert e4.max() <= 1.1 * e1.max(), (e1, e4)
+    assert np.all(i4 <= 1.3 * i1), (i1, i4)
+    # the rebuild evaluations (steps 4 and 8) see the same kind of tree
+    assert abs(e4[3] - e1[3]) <= 0.2 * e1[3]
+
+
+def test_tree_reuse_rebuilds_after_load(nb):
+    """A load replaces the bodies: the next evaluation rebuilds, so the forces
+    equal those of a fresh simulation bit for bit."""
+    n = 5000
+    a_st, b_st = nb.plummer(n, seed=1), nb.plummer(n, seed=2)
+    cfg = nb.Config(method=nb.BARNES_HUT, softening=1e-2, theta=0.6, flags=nb.bh_reuse_flag(8))
+    with nb.Sim(cfg, capacity=n) as s:
+        s.load(*a_st)
+        s.compute_forces()
+        s.load(*b_st)
+        s.compute_forces()
+        got = s.accelerations()
+    with nb.Sim(cfg, capacity=n) as f:
+        f.load(*b_st)
+        f.compute_forces()
+        want = f.accelerations()
+    for u, v in zip(got, want):
+        assert np.array_equal(u, v)
