@@ -11,7 +11,8 @@
 // origin and stages every j-chunk (32 consecutive sorted bodies, one per lane)
 // as a normalised double-single (S, E) of x - c.  A chunk whose bounding box
 // lies at least kFarFactor * D from the warp's box (D: the warp box diameter)
-// runs the plain FP32 term on S alone (15 FP32 operations + 1 MUFU); other
+// runs the plain FP32 term on S alone (15 FP32 operations + 1 MUFU), and a
+// chunk at least D/2 away drops the folded Newton step too (12 + 1); other
 // chunks take the full double-single term on S and E (21 + 1).  Decisions are
 // uniform over the warp (no divergence) and a warp stages its own chunks in its
 // own shared memory: no CTA-wide barrier.
@@ -30,10 +31,16 @@
 // displacement error is at most 2^-24 (2r + D) <= 2^-24 r (2 + 1/kFarFactor)
 // = 6 * 2^-24 r for kFarFactor = 1/4 -- about 3.6e-7 relative at worst, the
 // order of the FP32 arithmetic of the term (measured on a 65,536-body Plummer
-// sphere, factors 1/2, 1/4 and 1/8 leave the RMS force error at 3.2e-8).  Near terms keep the double-single
-// displacement (absolute error ~2^-48 |x|).  The folded Newton step on the
-// MUFU rsqrt is kept; every FP32 accumulator takes 32 terms before its
-// Kahan-compensated add, and the segments combine as a double-single.
+// sphere, factors 1/2, 1/4 and 1/8 leave the RMS force error at 3.2e-8).  A
+// very far term (gap >= D/2: displacement error <= 4 * 2^-24 r) also carries
+// the MUFU rsqrt error three times, at most 3.7e-7 and on average -1.6e-8
+// relative (measured over every FP32 input in [1, 4), i.e. every mantissa at
+// both exponent parities); these terms are many and distant,
+// so their errors average out: on the same sphere the maximum relative force
+// error stays at 7e-7 and the RMS at 3e-8.  Near terms keep the double-single
+// displacement (absolute error ~2^-48 |x|) and the Newton step; every FP32
+// accumulator takes 32 terms before its Kahan-compensated add, and the
+// segments combine as a double-single.
 #include "nb_internal.h"
 #include "nb_pair.cuh"
 
@@ -48,6 +55,7 @@ namespace {
 
 constexpr int kChunk = 32;             // j-chunk = one body per lane
 constexpr float kFarFactor2 = 0.0625f; // (gap / D)^2 threshold: kFarFactor = 1/4
+constexpr float kVeryFar2 = 0.25f;      // (gap / D)^2 threshold without Newton: 1/2
 constexpr int kResortEvals = 8;        // force evaluations per Morton re-sort
 
 // Positions in Morton order relative to the root centre, split into
@@ -139,9 +147,11 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
         }
     const float cx = 0.5f * (bmn[0] + bmx[0]), cy = 0.5f * (bmn[1] + bmx[1]),
                 cz = 0.5f * (bmn[2] + bmx[2]);
-    const float thr2 = far2 * ((bmx[0] - bmn[0]) * (bmx[0] - bmn[0]) +
-                               (bmx[1] - bmn[1]) * (bmx[1] - bmn[1]) +
-                               (bmx[2] - bmn[2]) * (bmx[2] - bmn[2]));
+    const float diam2 = (bmx[0] - bmn[0]) * (bmx[0] - bmn[0]) +
+                        (bmx[1] - bmn[1]) * (bmx[1] - bmn[1]) +
+                        (bmx[2] - bmn[2]) * (bmx[2] - bmn[2]);
+    const float thr2 = far2 * diam2;           // far: double-single not needed
+    const float thr2v = kVeryFar2 * diam2;     // very far: Newton step not needed
 
     // i-bodies relative to c, negated and duplicated into pairs
     float2 nsx[IPT], nsy[IPT], nsz[IPT], nex[IPT], ney[IPT], nez[IPT];
@@ -188,6 +198,7 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
         const float gz = fmaxf(0.f, fmaxf(jmn.z - bmx[2], bmn[2] - jmx.z));
         const float gap2 = gx * gx + gy * gy + gz * gz;
         const bool far = gap2 > 0.f && gap2 >= thr2;
+        const bool vfar = far && gap2 >= thr2v;
 
         // lanes past n stage a massless body far away: its terms are exactly 0
         float Sx = 1.0e18f, Sy = 1.0e18f, Sz = 1.0e18f, Ex = 0.f, Ey = 0.f, Ez = 0.f, mj = 0.f;
@@ -206,16 +217,24 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
             l = lo[(jc + 1) * kChunk + lane];
         }
 
-        if (far) {
+        if (vfar) {
 #pragma unroll 4
             for (int p = 0; p < kChunk / 2; ++p) {
                 const JPair j = pair_tile_get(sg, p);
 #pragma unroll
                 for (int k = 0; k < IPT; ++k)
-                    pair_term2_far(j, nsx[k], nsy[k], nsz[k], e2, ax[k], ay[k], az[k]);
+                    pair_term2_far<false>(j, nsx[k], nsy[k], nsz[k], e2, ax[k], ay[k], az[k]);
+            }
+        } else if (far) {
+#pragma unroll 4
+            for (int p = 0; p < kChunk / 2; ++p) {
+                const JPair j = pair_tile_get(sg, p);
+#pragma unroll
+                for (int k = 0; k < IPT; ++k)
+                    pair_term2_far<true>(j, nsx[k], nsy[k], nsz[k], e2, ax[k], ay[k], az[k]);
             }
         } else {
-#pragma unroll 2
+#pragma unroll 4
             for (int p = 0; p < kChunk / 2; ++p) {
                 const JPair j = pair_tile_get(sg, p);
 #pragma unroll
