@@ -126,17 +126,21 @@ def test_mixed_close_pairs_far_from_origin(nb, oracle):
     check_mixed(oracle, a, ref, st, 1.0, 1e-4)
 
 
-SORTED = ["plummer20000", "diskbulge16384", "cube10000_eps0", "pairs_far_origin_10000"]
+SORTED = ["plummer20000", "diskbulge16384", "cube10000_eps0", "pairs_far_origin_10000",
+          "plummer65536"]
 
 
 @pytest.mark.parametrize("name", SORTED)
 def test_mixed_sorted_near_far(nb, oracle, name):
     """N >= 8192 runs the Morton-sorted near/far variant of the mixed kernel:
-    far j-tiles use FP32 coordinates relative to the i-block centre, near
-    tiles the double-single displacement.  Same tolerances."""
+    far j-chunks use FP32 coordinates relative to the warp's centre (very far
+    ones without the Newton step), near chunks the double-single displacement.
+    Same tolerances."""
     G, eps = 1.0, 1e-3
     if name == "plummer20000":
         st = nb.plummer(20000, seed=4)
+    elif name == "plummer65536":  # the benchmark workload (eps 1e-3, seed 0)
+        st = nb.plummer(65536, seed=0)
     elif name == "diskbulge16384":
         st = nb.disk_bulge(16384, seed=5)
     elif name == "cube10000_eps0":
