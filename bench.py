@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=1.0,
                     help="seconds of Poisson arrivals for the serving extra (0 skips it)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--drift-steps", type=int, default=200,
+                    help="velocity-Verlet steps of the mixed vs FP64 energy-drift comparison "
+                         "(0 skips it; the target is stated over 1000)")
     ap.add_argument("--only", choices=["bh", "ensemble", "serving"], default=None,
                     help="run one extra workload alone and print its record (profiling)")
     return ap.parse_args()
@@ -189,6 +192,24 @@ def cpu_reference_rate(n, target_seconds, threads=0):
     dt = max(time.perf_counter() - t0, 1e-6)
     rows = int(min(n, max(256, rows * target_seconds / dt)))
     return x, y, z, m, rows, cores, O
+
+
+def energy_drift_pair(nb, n, steps, stream):
+    """Relative drift of the softened total energy over `steps` velocity-Verlet
+    steps of the bench workload, mixed path and FP64 path from the same start."""
+    state = nb.plummer(n, seed=SEED)
+    out = {"steps": steps, "dt": DT}
+    for name, method in (("mixed", nb.DIRECT_MIXED), ("fp64", nb.DIRECT_FP64)):
+        sim = nb.Sim(nb.Config(method=method, G=1.0, softening=EPS), capacity=n,
+                     stream=stream.cuda_stream)
+        sim.load(*state)
+        e0 = sim.diagnostics()["total_softened"]
+        sim.step(nb.VELOCITY_VERLET, DT, steps)
+        e1 = sim.diagnostics()["total_softened"]
+        sim.close()
+        out[name] = (e1 - e0) / abs(e0)
+    out["ratio_mixed_over_fp64"] = abs(out["mixed"]) / max(abs(out["fp64"]), 1e-300)
+    return out
 
 
 def pair_abs_sums(st, torch, tile=2048):
@@ -567,6 +588,8 @@ def run_ours(a, rank, world, local_rank):
                                  "mixed_speedup": achieved / fp64_rate}
         extras["gpu_baseline"] = reference_gpu_kernel_rate(st, n, inter, achieved, torch,
                                                            stream)
+        if a.drift_steps > 0:
+            extras["energy_drift_vs_fp64"] = energy_drift_pair(nb, n, a.drift_steps, stream)
 
     if not a.skip_extras and rank == 0 and a.bh_steps > 0:
         extras["barnes_hut"] = run_bh(a, nb, torch, dev, stream, flush, np)
