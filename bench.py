@@ -194,6 +194,20 @@ def cpu_reference_rate(n, target_seconds, threads=0):
     return x, y, z, m, rows, cores, O
 
 
+def max_over_ranks(local_ms: float, world: int, torch, device) -> float:
+    """The job's elapsed time: the maximum of the ranks' times (all ranks call)."""
+    if world <= 1:
+        return local_ms
+    t = torch.tensor([local_ms], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_rank: float, job_ms: float, world: int) -> float:
+    """Whole-job rate in G units/s: every replica processes units_per_rank."""
+    return world * units_per_rank / (job_ms / 1e3) / 1e9
+
+
 def energy_drift_pair(nb, n, steps, stream):
     """Relative drift of the softened total energy over `steps` velocity-Verlet
     steps of the bench workload, mixed path and FP64 path from the same start."""
@@ -512,12 +526,36 @@ def run_ours(a, rank, world, local_rank):
     sim.profile(False)
     clocks.stop()
     step_ms = [e0.elapsed_time(e1) for e0, e1 in zip(ev0, ev1)]
-    total_ms = sum(step_ms)
+    total_ms = max_over_ranks(sum(step_ms), world, torch, dev)
+    value = replica_rate(a.steps * inter, total_ms, world)
+    # the evolved state, before the end-to-end loop below reloads the start
+    e_end = None if a.skip_extras else sim.diagnostics()
+    evolved = None if a.skip_extras else sim.read_state()
+
+    # e2e: the same force evaluation through the C ABI with pinned host buffers
+    # (H2D of the inputs and D2H of the accelerations every step), every rank,
+    # max wall time over ranks
+    host = [torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for v in state]
+    outs = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(3)]
+    ptr_in = [h.data_ptr() for h in host]
+    ptr_out = [0] * 6 + [o.data_ptr() for o in outs] + [0]
+    for _ in range(max(1, a.warmup)):
+        sim.load_pointers(n, ptr_in)
+        sim.compute_forces()
+        sim.read_pointers(ptr_out)
+    ke = min(a.steps, 200)
     if world > 1:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * a.steps * inter / (total_ms / 1e3) / 1e9
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        sim.load_pointers(n, ptr_in)
+        sim.compute_forces()
+        sim.read_pointers(ptr_out)
+    el_ms = max_over_ranks((time.perf_counter() - t0) * 1e3, world, torch, dev)
+    e2e = {"value": replica_rate(ke * inter, el_ms, world), "unit": UNIT,
+           "h2d_bytes_per_step": 7 * 8 * n, "d2h_bytes_per_step": 3 * 8 * n,
+           "step": "nb_load (7 FP64 arrays) + nb_compute_forces + nb_read_state "
+                   "(3 acceleration arrays), pinned host memory, wall clock"}
 
     # roofline of the dominant kernel (the all-pairs kernel)
     props = torch.cuda.get_device_properties(local_rank)
@@ -545,7 +583,6 @@ def run_ours(a, rank, world, local_rank):
 
     extras = {}
     if not a.skip_extras and rank == 0:
-        e_end = sim.diagnostics()
         extras["energy_drift"] = {
             "steps": a.warmup + a.steps,
             "rel": (e_end["total_softened"] - e_start["total_softened"]) /
@@ -554,7 +591,8 @@ def run_ours(a, rank, world, local_rank):
         # accuracy and speed of the mixed kernel vs the FP64 kernel on the
         # current state (the FP64 path is pinned to the CPU oracle at 1e-12 by
         # the tests)
-        st = sim.read_state()
+        st = evolved
+        sim.load(st["x"], st["y"], st["z"], st["vx"], st["vy"], st["vz"], st["m"])
         sim.compute_forces()
         mixed_acc = sim.accelerations()
         ref = nb.Sim(nb.Config(method=nb.DIRECT_FP64, G=1.0, softening=EPS), capacity=n,
@@ -597,29 +635,6 @@ def run_ours(a, rank, world, local_rank):
         extras["ensemble"] = run_ensemble(a, nb, torch, stream)
     if not a.skip_extras and rank == 0 and a.serve_seconds > 0:
         extras["serving"] = run_serving(a, nb, np)
-
-    # e2e: one force evaluation through the C ABI with pinned host buffers
-    e2e = None
-    if rank == 0:
-        host = [torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for v in state]
-        outs = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(3)]
-        ptr_in = [h.data_ptr() for h in host]
-        ptr_out = [0] * 6 + [o.data_ptr() for o in outs] + [0]
-        for _ in range(max(1, a.warmup)):
-            sim.load_pointers(n, ptr_in)
-            sim.compute_forces()
-            sim.read_pointers(ptr_out)
-        ke = min(a.steps, 200)
-        t0 = time.perf_counter()
-        for _ in range(ke):
-            sim.load_pointers(n, ptr_in)
-            sim.compute_forces()
-            sim.read_pointers(ptr_out)
-        el = time.perf_counter() - t0
-        e2e = {"value": ke * inter / el / 1e9, "unit": UNIT, "h2d_bytes_per_step": 7 * 8 * n,
-               "d2h_bytes_per_step": 3 * 8 * n,
-               "step": "nb_load (7 FP64 arrays) + nb_compute_forces + nb_read_state "
-                       "(3 acceleration arrays), pinned host memory, wall clock"}
 
     cpu = None
     if rank == 0 and not a.skip_extras:
