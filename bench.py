@@ -322,7 +322,8 @@ def run_bh(a, nb, torch, dev, stream, flush, np):
     a.bh_steps leapfrog steps (CUDA events per step, L2 flushed before each),
     the walk kernel's share and rate, and the force error against the mixed
     direct sum; then the same with the tree rebuilt every 4 evaluations and
-    refitted in between (NB_FLAG_BH_REUSE(4))."""
+    refitted in between (NB_FLAG_BH_REUSE(4)), and with quadrupole moments
+    (NB_FLAG_BH_QUADRUPOLE)."""
     n = a.bh_n
     state = nb.disk_bulge(n, seed=SEED)
 
@@ -383,10 +384,12 @@ def run_bh(a, nb, torch, dev, stream, flush, np):
     out.update(timed(0))
     out["timing"] = ("CUDA events per leapfrog step, L2 flushed before each; a build reads "
                      "the node count on the host once per step")
+    keys = ("ms_per_step", "steps_per_s", "walk_ms", "interactions_per_body",
+            "force_error_vs_direct")
     reuse = timed(nb.bh_reuse_flag(4))
-    out["tree_reuse_4"] = {k: reuse[k] for k in ("ms_per_step", "steps_per_s", "walk_ms",
-                                                 "interactions_per_body",
-                                                 "force_error_vs_direct")}
+    out["tree_reuse_4"] = {k: reuse[k] for k in keys}
+    quad = timed(nb.BH_QUADRUPOLE)
+    out["quadrupole"] = {k: quad[k] for k in keys}
     return out
 
 

@@ -93,6 +93,11 @@ typedef struct nb_config {
  * change or a checkpoint restore forces a rebuild. */
 #define NB_FLAG_BH_REUSE(k) (((k) & 0xff) << 8)
 #define NB_FLAG_BH_REUSE_OF(flags) (((flags) >> 8) & 0xff)
+/* Barnes-Hut quadrupole moments: an accepted cell acts as its monopole plus its
+ * traceless quadrupole about the centre of mass (from FP64 prefix sums of the
+ * second moments).  The opening test is unchanged, so at the same theta the
+ * force error drops (the reference is monopole-only). */
+#define NB_FLAG_BH_QUADRUPOLE 2
 
 typedef struct nb_sim nb_sim;
 

@@ -349,6 +349,23 @@ gather_kernel(const uint32_t *__restrict__ order, const double *__restrict__ x,
     moments[i] = D4{mm, mm * rx, mm * ry, mm * rz};
 }
 
+// Second moments m x x^T (relative to the root centre) of every sorted body,
+// for the quadrupoles: a = (m x x, m y y, m z z, m x y), b = (m x z, m y z, 0, 0).
+__global__ void __launch_bounds__(256)
+gather2_kernel(const uint32_t *__restrict__ order, const double *__restrict__ x,
+               const double *__restrict__ y, const double *__restrict__ z,
+               const double *__restrict__ m, int n, const BHRoot *__restrict__ root,
+               D4 *__restrict__ ma, D4 *__restrict__ mb)
+{
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = order[i];
+    const double rx = x[o] - root->cx, ry = y[o] - root->cy, rz = z[o] - root->cz;
+    const double mm = m[o];
+    ma[i] = D4{mm * rx * rx, mm * ry * ry, mm * rz * rz, mm * rx * ry};
+    mb[i] = D4{mm * rx * rz, mm * ry * rz, 0.0, 0.0};
+}
+
 // ------------------------------------------------------------ scans (fixed order)
 template <class T> struct Add;
 template <> struct Add<int> {
@@ -633,16 +650,51 @@ refit_level_kernel(BHNode *__restrict__ nodes, int num_nodes,
     nodes[k].size2 = fmaxf(root->size2[d], box_ext2(mn, mx));
 }
 
+// ------------------------------------------------------------ quadrupoles
+// Traceless quadrupole of every node about its centre of mass, from the FP64
+// prefix sums of the moments: with S = sum m x x^T - M c c^T (positions
+// relative to the root centre, c the centre of mass),
+// Q = 3 S - tr(S) I; stored as (Qxx, Qyy, Qzz, Qxy), (Qxz, Qyz, 0, 0).
+__global__ void __launch_bounds__(256)
+quad_kernel(const BHNode *__restrict__ nodes, int num_nodes, const D4 *__restrict__ P,
+            const D4 *__restrict__ PA, const D4 *__restrict__ PB, float4 *__restrict__ quad)
+{
+    const int k = blockIdx.x * 256 + threadIdx.x;
+    if (k >= num_nodes) return;
+    const int a = nodes[k].first, b = a + nodes[k].count;
+    const double M = P[b].x - P[a].x;
+    float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
+    if (M > 0.0) {
+        const double cx = (P[b].y - P[a].y) / M, cy = (P[b].z - P[a].z) / M,
+                     cz = (P[b].w - P[a].w) / M;
+        const double sxx = (PA[b].x - PA[a].x) - M * cx * cx;
+        const double syy = (PA[b].y - PA[a].y) - M * cy * cy;
+        const double szz = (PA[b].z - PA[a].z) - M * cz * cz;
+        const double sxy = (PA[b].w - PA[a].w) - M * cx * cy;
+        const double sxz = (PB[b].x - PB[a].x) - M * cx * cz;
+        const double syz = (PB[b].y - PB[a].y) - M * cy * cz;
+        const double tr = sxx + syy + szz;
+        q0 = make_float4((float)(3.0 * sxx - tr), (float)(3.0 * syy - tr),
+                         (float)(3.0 * szz - tr), (float)(3.0 * sxy));
+        q1 = make_float4((float)(3.0 * sxz), (float)(3.0 * syz), 0.f, 0.f);
+    }
+    quad[2 * k] = q0;
+    quad[2 * k + 1] = q1;
+}
+
 // ------------------------------------------------------------ walk
 constexpr int kWalkBlock = 128;
 
 // ZERO_SOFT: eps2 == 0, where the lane's own body (r2 == 0) contributes 0.
-template <bool ZERO_SOFT>
+// QUAD: accepted cells act as monopole + quadrupole, a = G M r / |r|^3 +
+// G (5/2 (r.Q r) r / |r|^2 - Q r) / |r|^5 with r from the body to the centre
+// of mass (softened |r| throughout).
+template <bool ZERO_SOFT, bool QUAD>
 __global__ void __launch_bounds__(kWalkBlock)
 walk_kernel(const BHNode *__restrict__ nodes, int num_nodes, const float4 *__restrict__ body,
             const uint32_t *__restrict__ order, int n, float theta2, float eps2, double G,
             double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
-            BHStats *__restrict__ stats)
+            BHStats *__restrict__ stats, const float4 *__restrict__ quad)
 {
     const int lane = threadIdx.x & 31;
     const int warp0 = (blockIdx.x * kWalkBlock + threadIdx.x) - lane;
@@ -701,10 +753,23 @@ walk_kernel(const BHNode *__restrict__ nodes, int num_nodes, const float4 *__res
             p2p += nd.count;
         } else {
             const float inv = rsqrt_mufu(d2 + eps2);
-            const float s = (nd.com_mass.w * inv) * (inv * inv);
+            const float inv2 = inv * inv;
+            const float s = (nd.com_mass.w * inv) * inv2;
             fx = fmaf(dx, s, fx);
             fy = fmaf(dy, s, fy);
             fz = fmaf(dz, s, fz);
+            if (QUAD) {
+                const float4 q0 = quad[2 * node], q1 = quad[2 * node + 1];
+                const float qx = fmaf(q0.x, dx, fmaf(q0.w, dy, q1.x * dz));
+                const float qy = fmaf(q0.w, dx, fmaf(q0.y, dy, q1.y * dz));
+                const float qz = fmaf(q1.x, dx, fmaf(q1.y, dy, q0.z * dz));
+                const float rqr = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
+                const float inv5 = (inv * inv2) * inv2;  // |r|^-5
+                const float f = 2.5f * rqr * inv2;
+                fx = fmaf(inv5, fmaf(f, dx, -qx), fx);
+                fy = fmaf(inv5, fmaf(f, dy, -qy), fy);
+                fz = fmaf(inv5, fmaf(f, dz, -qz), fz);
+            }
             ++m2p;
         }
         node = nd.skip;
@@ -746,7 +811,9 @@ struct BHTree {
     int n = 0;
     int num_nodes = 0;
     DevBuf part, root, keys0, keys1, vals0, vals1, hist, body, moments, prefix, chain_len,
-        chain_depth, offsets, scan_tmp, nodes, node_depth, boxes, stats;
+        chain_depth, offsets, scan_tmp, nodes, node_depth, boxes, stats, moments2a, moments2b,
+        prefix2a, prefix2b, quad;
+    bool with_quad = false;     // the nodes carry quadrupoles (quad, 2 float4 per node)
     const uint64_t *sorted_codes = nullptr;
     const uint32_t *order = nullptr;
     bool tree_valid = false;    // nodes/order describe a build of these bodies' count
@@ -766,7 +833,8 @@ void bh_destroy(BHTree *t)
     DevBuf *bufs[] = {&t->part, &t->root, &t->keys0, &t->keys1, &t->vals0, &t->vals1,
                       &t->hist, &t->body, &t->moments, &t->prefix, &t->chain_len,
                       &t->chain_depth, &t->offsets, &t->scan_tmp, &t->nodes, &t->node_depth,
-                      &t->boxes, &t->stats};
+                      &t->boxes, &t->stats, &t->moments2a, &t->moments2b, &t->prefix2a,
+                      &t->prefix2b, &t->quad};
     for (DevBuf *b : bufs) b->release();
     delete t;
 }
@@ -832,22 +900,53 @@ nb_status bh_morton_order(BHTree *t, const double *x, const double *y, const dou
     return NB_OK;
 }
 
+template <bool ZS, bool Q>
+void walk_launch(BHTree *t, int n, float theta2, float eps2, double G, double *ax, double *ay,
+                 double *az, cudaStream_t st)
+{
+    walk_kernel<ZS, Q><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
+        t->nodes.as<BHNode>(), t->num_nodes, t->body.as<float4>(), t->order, n, theta2, eps2, G,
+        ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>());
+}
+
 static nb_status launch_walk(BHTree *t, int n, double G, double eps2, double theta, double *ax,
                              double *ay, double *az, cudaStream_t st, const KernelTimer *timer)
 {
-    BHStats *stats = t->stats.as<BHStats>();
-    const uint32_t *order = t->order;
+    const float th2 = (float)(theta * theta), e2 = (float)eps2;
     if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
-    if (eps2 > 0.0)
-        walk_kernel<false><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
-            t->nodes.as<BHNode>(), t->num_nodes, t->body.as<float4>(), order, n,
-            (float)(theta * theta), (float)eps2, G, ax, ay, az, stats);
-    else
-        walk_kernel<true><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
-            t->nodes.as<BHNode>(), t->num_nodes, t->body.as<float4>(), order, n,
-            (float)(theta * theta), 0.0f, G, ax, ay, az, stats);
+    if (t->with_quad) {
+        if (eps2 > 0.0) walk_launch<false, true>(t, n, th2, e2, G, ax, ay, az, st);
+        else walk_launch<true, true>(t, n, th2, 0.0f, G, ax, ay, az, st);
+    } else {
+        if (eps2 > 0.0) walk_launch<false, false>(t, n, th2, e2, G, ax, ay, az, st);
+        else walk_launch<true, false>(t, n, th2, 0.0f, G, ax, ay, az, st);
+    }
     NB_LAUNCH_CHECK();
     if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
+    return NB_OK;
+}
+
+// Quadrupoles of every node of the current tree (after its monopole pass).
+static nb_status compute_quads(BHTree *t, const double *x, const double *y, const double *z,
+                               const double *m, int n, cudaStream_t st)
+{
+    const size_t N = (size_t)n;
+    const int nn = t->num_nodes;
+    NB_TRY(t->moments2a.reserve(sizeof(D4) * N));
+    NB_TRY(t->moments2b.reserve(sizeof(D4) * N));
+    NB_TRY(t->prefix2a.reserve(sizeof(D4) * (N + 1)));
+    NB_TRY(t->prefix2b.reserve(sizeof(D4) * (N + 1)));
+    NB_TRY(t->quad.reserve(sizeof(float4) * 2 * (size_t)nn));
+    gather2_kernel<<<div_up(n, 256), 256, 0, st>>>(t->order, x, y, z, m, n,
+                                                   t->root.as<BHRoot>(), t->moments2a.as<D4>(),
+                                                   t->moments2b.as<D4>());
+    NB_LAUNCH_CHECK();
+    NB_TRY(scan_exclusive<D4>(t->moments2a.as<D4>(), n, t->prefix2a.as<D4>(), t->scan_tmp, st));
+    NB_TRY(scan_exclusive<D4>(t->moments2b.as<D4>(), n, t->prefix2b.as<D4>(), t->scan_tmp, st));
+    quad_kernel<<<div_up(nn, 256), 256, 0, st>>>(t->nodes.as<BHNode>(), nn, t->prefix.as<D4>(),
+                                                 t->prefix2a.as<D4>(), t->prefix2b.as<D4>(),
+                                                 t->quad.as<float4>());
+    NB_LAUNCH_CHECK();
     return NB_OK;
 }
 
@@ -883,11 +982,13 @@ static nb_status refit(BHTree *t, const double *x, const double *y, const double
 nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *z,
                      const double *m, int n, double G, double eps2, double theta,
                      int leaf_capacity, double *ax, double *ay, double *az, cudaStream_t st,
-                     const KernelTimer *timer, int reuse)
+                     const KernelTimer *timer, int reuse, bool quad)
 {
     if (n <= 0) return NB_OK;
+    t->with_quad = quad;
     if (ax && reuse > 1 && t->tree_valid && t->n == n && t->evals_since_build < reuse) {
         NB_TRY(refit(t, x, y, z, m, n, st));
+        if (quad) NB_TRY(compute_quads(t, x, y, z, m, n, st));
         ++t->evals_since_build;
         return launch_walk(t, n, G, eps2, theta, ax, ay, az, st, timer);
     }
@@ -935,6 +1036,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
                                                 t->nodes.as<BHNode>(),
                                                 t->node_depth.as<unsigned char>(), stats);
     NB_LAUNCH_CHECK();
+    if (quad) NB_TRY(compute_quads(t, x, y, z, m, n, st));
     t->tree_valid = true;
     t->evals_since_build = 0;
     if (!ax) return NB_OK;

@@ -189,11 +189,12 @@ void bh_destroy(BHTree *t);
 // Builds the tree of (x,y,z,m) and, when ax != nullptr, walks it writing
 // G * acceleration (FP64) in the original body order.  reuse > 1: the tree is
 // rebuilt every `reuse` walks; the walks in between keep its topology and
-// refit monopoles and cell sides to the current positions.
+// refit monopoles and cell sides to the current positions.  quad: accepted
+// cells act with their quadrupole moments too.
 nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *z,
                      const double *m, int n, double G, double eps2, double theta,
                      int leaf_capacity, double *ax, double *ay, double *az, cudaStream_t st,
-                     const KernelTimer *timer = nullptr, int reuse = 1);
+                     const KernelTimer *timer = nullptr, int reuse = 1, bool quad = false);
 // The next bh_compute rebuilds (the bodies were replaced).
 void bh_invalidate(BHTree *t);
 nb_status bh_info(BHTree *t, cudaStream_t st, nb_bh_info *info);

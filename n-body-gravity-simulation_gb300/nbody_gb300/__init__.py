@@ -113,6 +113,9 @@ def kernel_launch_count() -> int:
     return int(lib().nb_kernel_launch_count())
 
 
+BH_QUADRUPOLE = 2  # NB_FLAG_BH_QUADRUPOLE
+
+
 def bh_reuse_flag(k: int) -> int:
     """NB_FLAG_BH_REUSE(k): rebuild the Barnes-Hut tree every k evaluations."""
     return (int(k) & 0xFF) << 8

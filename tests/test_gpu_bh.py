@@ -303,3 +303,58 @@ def test_tree_reuse_rebuilds_after_load(nb):
         want = f.accelerations()
     for u, v in zip(got, want):
         assert np.array_equal(u, v)
+
+
+@pytest.mark.parametrize("theta", [0.5, 0.8])
+@pytest.mark.parametrize("gen", ["plummer", "disk_bulge"])
+def test_quadrupole_improves_accuracy(nb, theta, gen):
+    """NB_FLAG_BH_QUADRUPOLE: the same tree and opening test, cells acting with
+    their quadrupoles too -- the error against the FP64 direct sum drops."""
+    n = 20000
+    st = nb.plummer(n, seed=8) if gen == "plummer" else nb.disk_bulge(n, seed=8)
+    eps = 1e-3
+
+    def forces(method, flags=0):
+        cfg = nb.Config(method=method, G=1.0, softening=eps, theta=theta, flags=flags)
+        with nb.Sim(cfg, capacity=n) as s:
+            s.load(*st)
+            s.compute_forces()
+            return s.accelerations(), (s.bh_info() if method == nb.BARNES_HUT else None)
+
+    ref, _ = forces(nb.DIRECT_FP64)
+    r = np.sqrt(sum(v * v for v in ref))
+
+    def err(a):
+        d = np.sqrt(sum((u - v) ** 2 for u, v in zip(a, ref)))
+        rel = d / r
+        return float(rel.mean()), float(np.quantile(rel, 0.99))
+
+    mono, info_m = forces(nb.BARNES_HUT)
+    quad, info_q = forces(nb.BARNES_HUT, nb.BH_QUADRUPOLE)
+    (m_mean, m_p99), (q_mean, q_p99) = err(mono), err(quad)
+    assert q_mean <= 0.6 * m_mean, (m_mean, q_mean)
+    assert q_p99 <= 0.8 * m_p99, (m_p99, q_p99)
+    # same tree, same walk
+    assert info_m["num_nodes"] == info_q["num_nodes"]
+    assert info_m["interactions_m2p"] == info_q["interactions_m2p"]
+
+
+def test_quadrupole_with_tree_reuse(nb):
+    n, dt = 20000, 2e-3
+    st = nb.disk_bulge(n, seed=9)
+    flags = nb.BH_QUADRUPOLE | nb.bh_reuse_flag(4)
+    cfg = nb.Config(method=nb.BARNES_HUT, G=1.0, softening=1e-3, theta=0.6, flags=flags)
+    with nb.Sim(cfg, capacity=n) as s, \
+            nb.Sim(nb.Config(method=nb.DIRECT_FP64, G=1.0, softening=1e-3), capacity=n) as ref:
+        s.load(*st)
+        errs = []
+        for _ in range(4):
+            s.step(nb.LEAPFROG, dt)
+            cur = s.read_state()
+            ref.load(cur["x"], cur["y"], cur["z"], cur["vx"], cur["vy"], cur["vz"], cur["m"])
+            ref.compute_forces()
+            a_ref = ref.accelerations()
+            d = np.sqrt(sum((cur[k] - v) ** 2 for k, v in zip(("ax", "ay", "az"), a_ref)))
+            errs.append(float(np.mean(d / np.sqrt(sum(v * v for v in a_ref)))))
+    # refit evaluations (2-4) as accurate as the build (1)
+    assert max(errs) <= 1.15 * errs[0], errs
