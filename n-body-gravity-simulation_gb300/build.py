@@ -91,7 +91,7 @@ def build(force: bool = False, verbose_ptxas: bool = False, jobs: int | None = N
     os.makedirs(OUT_DIR, exist_ok=True)
     if force or _newer(LIB, objs):
         tmp = LIB + ".tmp"
-        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -8,8 +8,11 @@
 //      - direct jobs (n < direct_max_n) live in one body pool and advance
 //        together: one per-body kick-drift and kick over the pool and one
 //        persistent batched force launch over all of them (nb_batch.cu);
-//      - Barnes-Hut jobs each own a simulation object and run on their own
-//        streams, overlapping with the direct batch and with each other;
+//      - Barnes-Hut jobs each own a simulation object and run on one of
+//        kBHStreams streams, each stream's jobs issued by its own host thread
+//        (a tree build reads its node count on the host, which then blocks
+//        only that stream's later jobs), overlapping with the direct batch and
+//        with each other;
 //   3. retires jobs that reached their step count (state copied to the host,
 //      memory returned).
 // A job's arithmetic does not depend on the other jobs of a tick (the batched
@@ -26,6 +29,8 @@
 #include <deque>
 #include <map>
 #include <memory>
+#include <string>
+#include <thread>
 #include <vector>
 
 namespace nb {
@@ -35,7 +40,7 @@ using Clock = std::chrono::steady_clock;
 
 constexpr size_t kDirectBytesPerBody = 10 * 8 + 32;  // FP64 planes + hi/lo mirror
 constexpr size_t kBHBytesPerBody = 320;              // state + sort + tree buffers (upper bound)
-constexpr int kBHStreams = 4;
+constexpr int kBHStreams = 8;
 
 struct Job {
     int64_t id = 0;
@@ -271,12 +276,42 @@ nb_status tick(nb_server *s)
     // BH streams wait for the tick start so that latencies share one origin
     for (int k = 0; k < kBHStreams; ++k)
         NB_CUDA_TRY(cudaStreamWaitEvent(s->bh_streams[k], s->tick_start, 0));
-    // Barnes-Hut jobs first: their host-side node-count read would otherwise
-    // wait behind the direct batch on the device
-    for (Job *j : bh) {
-        NB_TRY(nb_step(j->sim, NB_LEAPFROG, dt, 1));
-        NB_CUDA_TRY(cudaEventRecord(j->step_done, s->bh_streams[j->stream_index]));
-    }
+    // Barnes-Hut jobs: one host thread per busy stream; this thread issues the
+    // direct batch meanwhile
+    std::vector<std::vector<Job *>> per_stream(kBHStreams);
+    for (Job *j : bh) per_stream[j->stream_index].push_back(j);
+    std::vector<nb_status> bh_status(kBHStreams, NB_OK);
+    std::vector<std::string> bh_error(kBHStreams);
+    int device = 0;
+    NB_CUDA_TRY(cudaGetDevice(&device));
+    auto run_stream = [&](int k) {
+        if (cudaSetDevice(device) != cudaSuccess) {
+            bh_status[k] = NB_ERR_CUDA;
+            bh_error[k] = "cudaSetDevice failed in a Barnes-Hut stream thread";
+            return;
+        }
+        for (Job *j : per_stream[k]) {
+            nb_status r = nb_step(j->sim, NB_LEAPFROG, dt, 1);
+            if (r == NB_OK && cudaEventRecord(j->step_done, s->bh_streams[k]) != cudaSuccess)
+                r = cuda_fail(cudaGetLastError(), "cudaEventRecord");
+            if (r != NB_OK) {
+                bh_status[k] = r;
+                bh_error[k] = nb_last_error();
+                return;
+            }
+        }
+    };
+    std::vector<std::thread> workers;
+    for (int k = 0; k < kBHStreams; ++k)
+        if (!per_stream[k].empty()) workers.emplace_back(run_stream, k);
+    struct Joiner {
+        std::vector<std::thread> &w;
+        ~Joiner()
+        {
+            for (auto &t : w)
+                if (t.joinable()) t.join();
+        }
+    } joiner{workers};
     if (!direct.empty()) {
         float4 *hi = s->hi.as<float4>(), *lo = s->lo.as<float4>();
         if (!new_direct.empty()) {
@@ -299,6 +334,9 @@ nb_status tick(nb_server *s)
                     nullptr, nullptr, nullptr, s->stream));
         NB_CUDA_TRY(cudaEventRecord(s->direct_done, s->stream));
     }
+    for (auto &t : workers) t.join();
+    for (int k = 0; k < kBHStreams; ++k)
+        if (bh_status[k] != NB_OK) return fail(bh_status[k], bh_error[k]);
     NB_CUDA_TRY(cudaStreamSynchronize(s->stream));
     for (int k = 0; k < kBHStreams; ++k) NB_CUDA_TRY(cudaStreamSynchronize(s->bh_streams[k]));
     float tick_ms = 0.f;
