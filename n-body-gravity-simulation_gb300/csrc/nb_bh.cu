@@ -43,6 +43,7 @@
 #include "nb_pair.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -788,6 +789,140 @@ walk_kernel(const BHNode *__restrict__ nodes, int num_nodes, const float4 *__res
     }
 }
 
+// The same walk for 64 * NP consecutive sorted bodies per warp, 2 * NP per
+// lane (body w0 + 32 k + lane for k < 2 NP, held as NP packed pairs): one node
+// load, vote and branch serve them all, and their MAC, monopole and leaf terms
+// run as f32x2 pairs.  The warp opens a node if any of its bodies does --
+// never a coarser walk than any body's own.
+template <bool ZERO_SOFT, bool QUAD, int NP>
+__global__ void __launch_bounds__(kWalkBlock)
+walk2_kernel(const BHNode *__restrict__ nodes, int num_nodes, const float4 *__restrict__ body,
+             const uint32_t *__restrict__ order, int n, float theta2, float eps2, double G,
+             double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
+             BHStats *__restrict__ stats, const float4 *__restrict__ quad)
+{
+    constexpr int kPer = 64 * NP;  // bodies per warp
+    const int lane = threadIdx.x & 31;
+    const int w0 = ((blockIdx.x * kWalkBlock + threadIdx.x) >> 5) * kPer;
+    if (w0 >= n) return;  // whole warp past the end
+    int ia[NP], ib[NP];
+    bool va[NP], vb[NP];
+    float2 npx[NP], npy[NP], npz[NP], fx[NP], fy[NP], fz[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        ia[k] = w0 + 64 * k + lane;
+        ib[k] = ia[k] + 32;
+        va[k] = ia[k] < n;
+        vb[k] = ib[k] < n;
+        const float4 pa = body[va[k] ? ia[k] : n - 1], pb = body[vb[k] ? ib[k] : n - 1];
+        npx[k] = make_float2(-pa.x, -pb.x);
+        npy[k] = make_float2(-pa.y, -pb.y);
+        npz[k] = make_float2(-pa.z, -pb.z);
+        fx[k] = fy[k] = fz[k] = dup2(0.f);
+    }
+    const float2 e2 = dup2(eps2), t2 = dup2(theta2);
+    unsigned m2p = 0, p2p = 0;
+    int node = 0;
+    while (node < num_nodes) {
+        const BHNode nd = nodes[node];
+        float2 dx[NP], dy[NP], dz[NP], d2[NP];
+        bool open = false;
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            dx[k] = add2(dup2(nd.com_mass.x), npx[k]);
+            dy[k] = add2(dup2(nd.com_mass.y), npy[k]);
+            dz[k] = add2(dup2(nd.com_mass.z), npz[k]);
+            d2[k] = fma2(dz[k], dz[k], fma2(dy[k], dy[k], mul2(dx[k], dx[k])));
+            const float2 td2 = mul2(t2, d2[k]);
+            const bool oa = va[k] & (((unsigned)(ia[k] - nd.first) < (unsigned)nd.count) |
+                                     (nd.size2 >= td2.x));
+            const bool ob = vb[k] & (((unsigned)(ib[k] - nd.first) < (unsigned)nd.count) |
+                                     (nd.size2 >= td2.y));
+            open = open | oa | ob;
+        }
+        if (__any_sync(0xffffffffu, open)) {
+            if (nd.skip != node + 1) {  // internal: descend
+                ++node;
+                continue;
+            }
+            const int e = nd.first + nd.count;
+            for (int b = nd.first; b < e; ++b) {
+                const float4 q = body[b];
+#pragma unroll
+                for (int k = 0; k < NP; ++k) {
+                    const float2 rx = add2(dup2(q.x), npx[k]);
+                    const float2 ry = add2(dup2(q.y), npy[k]);
+                    const float2 rz = add2(dup2(q.z), npz[k]);
+                    const float2 r2 = fma2(rz, rz, fma2(ry, ry, fma2(rx, rx, e2)));
+                    float2 inv = make_float2(rsqrt_mufu(r2.x), rsqrt_mufu(r2.y));
+                    if (ZERO_SOFT) {
+                        inv.x = r2.x > 0.f ? inv.x : 0.f;
+                        inv.y = r2.y > 0.f ? inv.y : 0.f;
+                    }
+                    const float2 s = mul2(mul2(dup2(q.w), inv), mul2(inv, inv));
+                    fx[k] = fma2(rx, s, fx[k]);
+                    fy[k] = fma2(ry, s, fy[k]);
+                    fz[k] = fma2(rz, s, fz[k]);
+                }
+            }
+            p2p += nd.count;
+        } else {
+            float4 q0, q1;
+            if (QUAD) {
+                q0 = quad[2 * node];
+                q1 = quad[2 * node + 1];
+            }
+#pragma unroll
+            for (int k = 0; k < NP; ++k) {
+                const float2 r2 = add2(d2[k], e2);
+                const float2 inv = make_float2(rsqrt_mufu(r2.x), rsqrt_mufu(r2.y));
+                const float2 inv2 = mul2(inv, inv);
+                const float2 s = mul2(mul2(dup2(nd.com_mass.w), inv), inv2);
+                fx[k] = fma2(dx[k], s, fx[k]);
+                fy[k] = fma2(dy[k], s, fy[k]);
+                fz[k] = fma2(dz[k], s, fz[k]);
+                if (QUAD) {
+                    const float2 qx = fma2(dup2(q0.x), dx[k],
+                                           fma2(dup2(q0.w), dy[k], mul2(dup2(q1.x), dz[k])));
+                    const float2 qy = fma2(dup2(q0.w), dx[k],
+                                           fma2(dup2(q0.y), dy[k], mul2(dup2(q1.y), dz[k])));
+                    const float2 qz = fma2(dup2(q1.x), dx[k],
+                                           fma2(dup2(q1.y), dy[k], mul2(dup2(q0.z), dz[k])));
+                    const float2 rqr = fma2(dx[k], qx, fma2(dy[k], qy, mul2(dz[k], qz)));
+                    const float2 inv5 = mul2(mul2(inv, inv2), inv2);
+                    const float2 f = mul2(mul2(dup2(2.5f), rqr), inv2);
+                    fx[k] = fma2(inv5, fma2(f, dx[k], make_float2(-qx.x, -qx.y)), fx[k]);
+                    fy[k] = fma2(inv5, fma2(f, dy[k], make_float2(-qy.x, -qy.y)), fy[k]);
+                    fz[k] = fma2(inv5, fma2(f, dz[k], make_float2(-qz.x, -qz.y)), fz[k]);
+                }
+            }
+            ++m2p;
+        }
+        node = nd.skip;
+    }
+    unsigned nv = 0;
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        if (va[k]) {
+            const uint32_t o = order[ia[k]];
+            ax[o] = G * (double)fx[k].x;
+            ay[o] = G * (double)fy[k].x;
+            az[o] = G * (double)fz[k].x;
+        }
+        if (vb[k]) {
+            const uint32_t o = order[ib[k]];
+            ax[o] = G * (double)fx[k].y;
+            ay[o] = G * (double)fy[k].y;
+            az[o] = G * (double)fz[k].y;
+        }
+        nv += __popc(__ballot_sync(0xffffffffu, va[k])) + __popc(__ballot_sync(0xffffffffu, vb[k]));
+    }
+    if (lane == 0) {
+        atomicAdd(&stats->m2p, (unsigned long long)m2p * nv);
+        atomicAdd(&stats->p2p, (unsigned long long)p2p * nv);
+    }
+}
+
 int div_up(long a, long b) { return (int)((a + b - 1) / b); }
 
 template <class T>
@@ -900,13 +1035,35 @@ nb_status bh_morton_order(BHTree *t, const double *x, const double *y, const dou
     return NB_OK;
 }
 
+// Packed body pairs per lane of the walk (0: the one-body-per-lane walk);
+// NB_BH_WALK_PAIRS overrides the default.
+int walk_pairs()
+{
+    static const int np = [] {
+        const char *e = std::getenv("NB_BH_WALK_PAIRS");
+        const int v = e ? std::atoi(e) : 1;
+        return v < 0 ? 0 : (v > 2 ? 2 : v);
+    }();
+    return np;
+}
+
 template <bool ZS, bool Q>
 void walk_launch(BHTree *t, int n, float theta2, float eps2, double G, double *ax, double *ay,
                  double *az, cudaStream_t st)
 {
-    walk_kernel<ZS, Q><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
-        t->nodes.as<BHNode>(), t->num_nodes, t->body.as<float4>(), t->order, n, theta2, eps2, G,
-        ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>());
+    const int np = walk_pairs();
+    if (np == 2)
+        walk2_kernel<ZS, Q, 2><<<div_up(n, 4 * kWalkBlock), kWalkBlock, 0, st>>>(
+            t->nodes.as<BHNode>(), t->num_nodes, t->body.as<float4>(), t->order, n, theta2,
+            eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>());
+    else if (np == 1)
+        walk2_kernel<ZS, Q, 1><<<div_up(n, 2 * kWalkBlock), kWalkBlock, 0, st>>>(
+            t->nodes.as<BHNode>(), t->num_nodes, t->body.as<float4>(), t->order, n, theta2,
+            eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>());
+    else
+        walk_kernel<ZS, Q><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
+            t->nodes.as<BHNode>(), t->num_nodes, t->body.as<float4>(), t->order, n, theta2,
+            eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>());
 }
 
 static nb_status launch_walk(BHTree *t, int n, double G, double eps2, double theta, double *ax,
