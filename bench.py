@@ -581,6 +581,9 @@ def run_ours(a, rank, world, local_rank):
     if clk.get("sm_mhz"):
         roofline["frac_at_measured_clock"] = achieved / fp32_roofline_gint(
             props.multi_processor_count, clk["sm_mhz"])
+    # the same fraction in FP32-pipe operations per second (12 per interaction)
+    roofline["achieved_fp32_tops"] = achieved * 12.0 / 1e3
+    roofline["peak_fp32_tops"] = peak * 12.0 / 1e3
     roofline["traffic"] = profiled_traffic("direct_sorted_n65536.md") if n == N_BODIES else None
     roofline["algorithmic_bytes"] = 32 * n  # hi + lo mirror of every body, read once
 
