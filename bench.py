@@ -194,6 +194,36 @@ def cpu_reference_rate(n, target_seconds, threads=0):
     return x, y, z, m, rows, cores, O
 
 
+def run_plain(nb, torch, stream):
+    """The reference's CPU-runnable configuration on the GPU: N = 1024 Plummer
+    (seed 0), FP64 direct sum, softening 0.01, leapfrog KDK dt = 1e-3, 100
+    steps (its parity with the oracle is a GPU test); CUDA events around the
+    100 steps after one untimed run of the same configuration."""
+    n, steps = 1024, 100
+    state = nb.plummer(n, seed=SEED)
+    cfg = nb.Config(method=nb.DIRECT_FP64, G=1.0, softening=0.01)
+    out = {}
+    for timed in (False, True):
+        sim = nb.Sim(cfg, capacity=n, stream=stream.cuda_stream)
+        sim.load(*state)
+        e0 = sim.diagnostics()["total_softened"]
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        sim.step(nb.LEAPFROG, 1e-3, steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        e1 = sim.diagnostics()["total_softened"]
+        sim.close()
+        if timed:
+            ms = ev0.elapsed_time(ev1) / steps
+            out = {"workload": "plummer_n1024_fp64_direct_leapfrog_100_steps", "n": n,
+                   "steps": steps, "ms_per_step": ms, "steps_per_s": 1e3 / ms,
+                   "ginteractions_s": n * (n - 1) / (ms / 1e3) / 1e9,
+                   "energy_rel_change": (e1 - e0) / abs(e0)}
+    return out
+
+
 def max_over_ranks(local_ms: float, world: int, torch, device) -> float:
     """The job's elapsed time: the maximum of the ranks' times (all ranks call)."""
     if world <= 1:
@@ -634,6 +664,7 @@ def run_ours(a, rank, world, local_rank):
                                                            stream)
         if a.drift_steps > 0:
             extras["energy_drift_vs_fp64"] = energy_drift_pair(nb, n, a.drift_steps, stream)
+        extras["plain_fp64_n1024"] = run_plain(nb, torch, stream)
 
     if not a.skip_extras and rank == 0 and a.bh_steps > 0:
         extras["barnes_hut"] = run_bh(a, nb, torch, dev, stream, flush, np)

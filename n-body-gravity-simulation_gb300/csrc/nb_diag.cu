@@ -75,20 +75,20 @@ potential_rows_kernel(const double *__restrict__ x, const double *__restrict__ y
                       const double *__restrict__ z, const double *__restrict__ m, int n,
                       double eps2, double *__restrict__ pu, double *__restrict__ ps)
 {
-    __shared__ double4 sh[kRed];
+    __shared__ double4_32a sh[kRed];
     const int i = blockIdx.x * kRed + threadIdx.x;
     const double xi = i < n ? x[i] : 0.0, yi = i < n ? y[i] : 0.0, zi = i < n ? z[i] : 0.0;
     double su = 0.0, ss = 0.0;
     for (int t0 = 0; t0 < n; t0 += kRed) {
         const int j = t0 + threadIdx.x;
         __syncthreads();
-        sh[threadIdx.x] = j < n ? make_double4(x[j], y[j], z[j], m[j])
-                                : make_double4(0.0, 0.0, 0.0, 0.0);
+        sh[threadIdx.x] = j < n ? make_double4_32a(x[j], y[j], z[j], m[j])
+                                : make_double4_32a(0.0, 0.0, 0.0, 0.0);
         __syncthreads();
         const int lim = min(kRed, n - t0);
         for (int jj = 0; jj < lim; ++jj) {
             if (t0 + jj == i) continue;
-            const double4 B = sh[jj];
+            const double4_32a B = sh[jj];
             const double dx = B.x - xi, dy = B.y - yi, dz = B.z - zi;
             const double r2 = dx * dx + dy * dy + dz * dz;
             su += B.w / sqrt(r2);

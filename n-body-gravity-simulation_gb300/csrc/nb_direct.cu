@@ -152,7 +152,7 @@ direct_fp64_kernel(const double *__restrict__ x, const double *__restrict__ y,
                    const double *__restrict__ z, const double *__restrict__ m, int n,
                    double eps2, int seg_len, double *__restrict__ part)
 {
-    __shared__ double4 sh[BLOCK];
+    __shared__ double4_32a sh[BLOCK];
     const int tid = threadIdx.x;
     const int ibase = blockIdx.x * (BLOCK * IPT);
     double xi[IPT], yi[IPT], zi[IPT], ax[IPT], ay[IPT], az[IPT];
@@ -168,14 +168,14 @@ direct_fp64_kernel(const double *__restrict__ x, const double *__restrict__ y,
     const int j1 = min(n, j0 + seg_len);
     for (int t0 = j0; t0 < j1; t0 += BLOCK) {
         const int j = t0 + tid;
-        double4 b = make_double4(1.0e150, 1.0e150, 1.0e150, 0.0);
-        if (j < j1) b = make_double4(x[j], y[j], z[j], m[j]);
+        double4_32a b = make_double4_32a(1.0e150, 1.0e150, 1.0e150, 0.0);
+        if (j < j1) b = make_double4_32a(x[j], y[j], z[j], m[j]);
         __syncthreads();
         sh[tid] = b;
         __syncthreads();
 #pragma unroll 2
         for (int jj = 0; jj < BLOCK; ++jj) {
-            const double4 B = sh[jj];
+            const double4_32a B = sh[jj];
 #pragma unroll
             for (int k = 0; k < IPT; ++k) {
                 const double dx = B.x - xi[k];
@@ -271,6 +271,7 @@ constexpr int kMixBlock = 256;
 constexpr int kMixIpt = 4;
 constexpr int kF64Block = 128;
 constexpr int kF64Ipt = 2;
+constexpr int kF64SmallMax = 8192;  // largest N of the one-warp FP64 shape
 
 // Tile shapes of the mixed kernel the autotuner chooses from: threads per CTA
 // x i-bodies per thread.  More i-bodies per thread amortise the two
@@ -462,37 +463,48 @@ nb_status direct_mixed(const float4 *hi, const float4 *lo, int n, double G, doub
     return NB_OK;
 }
 
-nb_status direct_fp64(const double *x, const double *y, const double *z, const double *m, int n,
-                      double G, double eps2, double *ax, double *ay, double *az,
-                      DevBuf &partials, cudaStream_t st, const KernelTimer *timer)
+template <int B, int I>
+static nb_status direct_fp64_shape(const double *x, const double *y, const double *z,
+                                   const double *m, int n, double G, double eps2, double *ax,
+                                   double *ay, double *az, DevBuf &partials, cudaStream_t st,
+                                   const KernelTimer *timer)
 {
-    if (n <= 0) return NB_OK;
-    const int per_cta = kF64Block * kF64Ipt;
+    const int per_cta = B * I;
     const int iblocks = (n + per_cta - 1) / per_cta;
-    const int tiles = (n + kF64Block - 1) / kF64Block;
+    const int tiles = (n + B - 1) / B;
     static int slots = 0;
-    if (!slots)
-        slots = resident_ctas<kF64Block, kF64Ipt>(
-            (const void *)direct_fp64_kernel<kF64Block, kF64Ipt, false>);
+    if (!slots) slots = resident_ctas<B, I>((const void *)direct_fp64_kernel<B, I, false>);
     int segs = pick_segments(iblocks, tiles, slots);
     const int seg_tiles = (tiles + segs - 1) / segs;
     segs = (tiles + seg_tiles - 1) / seg_tiles;
     NB_TRY(partials.reserve(sizeof(double) * 3 * (size_t)n * segs));
     double *part = partials.as<double>();
     dim3 grid(iblocks, segs);
-    const int seg_len = seg_tiles * kF64Block;
+    const int seg_len = seg_tiles * B;
     if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
     if (eps2 > 0.0)
-        direct_fp64_kernel<kF64Block, kF64Ipt, false>
-            <<<grid, kF64Block, 0, st>>>(x, y, z, m, n, eps2, seg_len, part);
+        direct_fp64_kernel<B, I, false><<<grid, B, 0, st>>>(x, y, z, m, n, eps2, seg_len, part);
     else
-        direct_fp64_kernel<kF64Block, kF64Ipt, true>
-            <<<grid, kF64Block, 0, st>>>(x, y, z, m, n, 0.0, seg_len, part);
+        direct_fp64_kernel<B, I, true><<<grid, B, 0, st>>>(x, y, z, m, n, 0.0, seg_len, part);
     NB_LAUNCH_CHECK();
     if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
     combine_fp64_kernel<<<(n + 255) / 256, 256, 0, st>>>(part, n, segs, G, ax, ay, az);
     NB_LAUNCH_CHECK();
     return NB_OK;
+}
+
+// Small systems take one-warp CTAs with 32-body j-tiles, so that up to
+// (N/32)^2 CTAs share the FP64 work (N = 1024 with the large shape fills only
+// 32 CTAs); large systems take 128 x 2.
+nb_status direct_fp64(const double *x, const double *y, const double *z, const double *m, int n,
+                      double G, double eps2, double *ax, double *ay, double *az,
+                      DevBuf &partials, cudaStream_t st, const KernelTimer *timer)
+{
+    if (n <= 0) return NB_OK;
+    if (n <= kF64SmallMax)
+        return direct_fp64_shape<32, 1>(x, y, z, m, n, G, eps2, ax, ay, az, partials, st, timer);
+    return direct_fp64_shape<kF64Block, kF64Ipt>(x, y, z, m, n, G, eps2, ax, ay, az, partials,
+                                                 st, timer);
 }
 
 } // namespace nb
