@@ -98,6 +98,12 @@ typedef struct nb_config {
  * second moments).  The opening test is unchanged, so at the same theta the
  * force error drops (the reference is monopole-only). */
 #define NB_FLAG_BH_QUADRUPOLE 2
+/* NB_DIRECT_MIXED kernel choice.  By default systems of at least 28,672 bodies
+ * take the Morton-sorted near/far kernel (far j-chunks in plain FP32 relative to
+ * a warp-local origin) and smaller ones the all-pairs double-single kernel;
+ * these flags force one or the other (same accuracy criteria either way). */
+#define NB_FLAG_MIXED_SORTED 4
+#define NB_FLAG_MIXED_UNSORTED 8
 
 typedef struct nb_sim nb_sim;
 

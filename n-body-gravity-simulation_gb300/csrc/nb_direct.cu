@@ -280,7 +280,8 @@ constexpr int kF64SmallMax = 8192;  // largest N of the one-warp FP64 shape
 struct MixShape {
     int block, ipt;
 };
-constexpr MixShape kMixShapes[] = {{256, 4}, {128, 2}, {128, 4}, {256, 2}, {64, 4}};
+constexpr MixShape kMixShapes[] = {{256, 4}, {128, 2}, {128, 4}, {256, 2}, {64, 4},
+                                    {32, 1}, {32, 2}};
 constexpr int kNumMixShapes = sizeof(kMixShapes) / sizeof(kMixShapes[0]);
 
 template <int B, int I>
@@ -298,6 +299,8 @@ int mix_slots_for(int block, int ipt)
     if (block == 128 && ipt == 4) return mix_slots<128, 4>();
     if (block == 256 && ipt == 2) return mix_slots<256, 2>();
     if (block == 64 && ipt == 4) return mix_slots<64, 4>();
+    if (block == 32 && ipt == 1) return mix_slots<32, 1>();
+    if (block == 32 && ipt == 2) return mix_slots<32, 2>();
     return 0;
 }
 
@@ -330,6 +333,10 @@ bool launch_mixed(const DirectPlan &p, cudaStream_t st, const float4 *hi, const 
         launch_mixed_shape<256, 2>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
     else if (p.block == 64 && p.ipt == 4)
         launch_mixed_shape<64, 4>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
+    else if (p.block == 32 && p.ipt == 1)
+        launch_mixed_shape<32, 1>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
+    else if (p.block == 32 && p.ipt == 2)
+        launch_mixed_shape<32, 2>(grid, st, hi, lo, n, eps2, seg_len, psum, pcomp);
     else
         return false;
     return true;
@@ -377,6 +384,8 @@ DirectPlan direct_mixed_plan(int n)
         auto it = g_tuned.find(n);
         if (it != g_tuned.end()) return it->second;
     }
+    // small systems (not tuned): one-warp CTAs, as many as the j-split allows
+    if (n < 4096) return plan_for_shape(n, 32, n < 2048 ? 1 : 2);
     return plan_for_shape(n, kMixBlock, kMixIpt);
 }
 

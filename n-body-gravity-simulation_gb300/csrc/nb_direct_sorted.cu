@@ -394,13 +394,15 @@ void SortedBuffers::release()
     order_n = -1;
 }
 
-bool direct_sorted_enabled(int n)
+bool direct_sorted_enabled(int n, int flags)
 {
+    if (flags & NB_FLAG_MIXED_UNSORTED) return false;
+    if (flags & NB_FLAG_MIXED_SORTED) return n > 0;
     static const bool on = [] {
         const char *e = std::getenv("NB_DIRECT_SORTED");
         return !(e && std::strcmp(e, "0") == 0);
     }();
-    return on && n >= 8192;
+    return on && n >= kSortedMinBodies;
 }
 
 static nb_status run_sorted(const DirectPlan &p, const float4 *hi, const float4 *lo, int n,

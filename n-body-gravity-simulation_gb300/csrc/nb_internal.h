@@ -111,7 +111,12 @@ nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
                               const double *m, int n, double G, double eps2, double *ax,
                               double *ay, double *az, SortedBuffers &b, cudaStream_t st,
                               const KernelTimer *timer = nullptr);
-bool direct_sorted_enabled(int n);
+// Whether an evaluation of n bodies takes the sorted variant: flags
+// NB_FLAG_MIXED_SORTED / NB_FLAG_MIXED_UNSORTED decide, else n >= kSortedMinBodies
+// (measured crossover on GB300: the sort and the near chunks cost more than the
+// far chunks save below ~28k bodies of a Plummer sphere).
+constexpr int kSortedMinBodies = 28672;
+bool direct_sorted_enabled(int n, int flags);
 
 // FP64 all-pairs kernel.
 nb_status direct_fp64(const double *x, const double *y, const double *z, const double *m,

@@ -107,7 +107,7 @@ nb_status eval_forces(nb_sim *s, const double *px, const double *py, const doubl
         return direct_fp64(px, py, pz, s->m(), n, s->cfg.G, eps2, oax, oay, oaz, s->partials,
                            s->stream, timer);
     case NB_DIRECT_MIXED: {
-        if (direct_sorted_enabled(n))
+        if (direct_sorted_enabled(n, s->cfg.flags))
             return direct_mixed_sorted(px, py, pz, s->m(), n, s->cfg.G, eps2, oax, oay, oaz,
                                        s->sorted, s->stream, timer);
         NB_TRY(s->split_hi.reserve(sizeof(float4) * s->capacity));

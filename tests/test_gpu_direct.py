@@ -58,9 +58,10 @@ def cube(oracle, n, seed=42):
     return x, y, z, np.zeros(n), np.zeros(n), np.zeros(n), m
 
 
-def gpu_forces(nb, method, state, G, eps):
+def gpu_forces(nb, method, state, G, eps, flags=0):
     n = len(state[0])
-    with nb.Sim(nb.Config(method=method, G=G, softening=eps), capacity=max(n, 1)) as s:
+    with nb.Sim(nb.Config(method=method, G=G, softening=eps, flags=flags),
+                capacity=max(n, 1)) as s:
         s.load(*state)
         s.compute_forces()
         return s.accelerations()
@@ -132,10 +133,10 @@ SORTED = ["plummer20000", "diskbulge16384", "cube10000_eps0", "pairs_far_origin_
 
 @pytest.mark.parametrize("name", SORTED)
 def test_mixed_sorted_near_far(nb, oracle, name):
-    """N >= 8192 runs the Morton-sorted near/far variant of the mixed kernel:
-    far j-chunks use FP32 coordinates relative to the warp's centre (very far
-    ones without the Newton step), near chunks the double-single displacement.
-    Same tolerances."""
+    """The Morton-sorted near/far variant of the mixed kernel (the default from
+    28,672 bodies, forced here by NB_FLAG_MIXED_SORTED): far j-chunks use FP32
+    coordinates relative to the warp's centre (very far ones without the Newton
+    step), near chunks the double-single displacement.  Same tolerances."""
     G, eps = 1.0, 1e-3
     if name == "plummer20000":
         st = nb.plummer(20000, seed=4)
@@ -153,9 +154,29 @@ def test_mixed_sorted_near_far(nb, oracle, name):
         st = (p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy(), z0, z0, z0,
               rng.uniform(0.5, 2.0, 10000))
         eps = 1e-4
-    a = gpu_forces(nb, nb.DIRECT_MIXED, st, G, eps)
+    a = gpu_forces(nb, nb.DIRECT_MIXED, st, G, eps, flags=nb.MIXED_SORTED)
     ref = oracle.forces_naive(st[0], st[1], st[2], st[6], G, eps)
     check_mixed(oracle, a, ref, st, G, eps)
+
+
+@pytest.mark.parametrize("n", [37, 1000, 3000])
+def test_mixed_sorted_small_and_ragged(nb, oracle, n):
+    """The sorted kernel on sizes that are not multiples of its 32-body chunks
+    or 64-body warps, and smaller than one warp's share."""
+    st = cube(oracle, n, seed=5)
+    a = gpu_forces(nb, nb.DIRECT_MIXED, st, 1.0, 0.01, flags=nb.MIXED_SORTED)
+    ref = oracle.forces_naive(st[0], st[1], st[2], st[6], 1.0, 0.01)
+    check_mixed(oracle, a, ref, st, 1.0, 0.01)
+
+
+def test_mixed_kernel_choice_flags(nb, oracle):
+    """Default, forced-sorted and forced-unsorted mixed kernels all meet the
+    tolerances on the same 30,000 bodies (the default is sorted there)."""
+    st = nb.plummer(30000, seed=6)
+    ref = oracle.forces_naive(st[0], st[1], st[2], st[6], 1.0, 1e-3)
+    for flags in (0, nb.MIXED_SORTED, nb.MIXED_UNSORTED):
+        a = gpu_forces(nb, nb.DIRECT_MIXED, st, 1.0, 1e-3, flags=flags)
+        check_mixed(oracle, a, ref, st, 1.0, 1e-3)
 
 
 @pytest.mark.parametrize("method", ["fp64", "mixed"])
