@@ -384,7 +384,8 @@ nb_status nb_checkpoint_save(nb_sim *sim, const char *path);
 /* Restores configuration, state and the accelerations flag; n must fit the
  * simulation's capacity.  Continuing after a restore gives the same bits as
  * continuing the saved run for the FP64 and Barnes-Hut methods and for the
- * mixed method below 8192 bodies; above, the mixed path re-sorts the bodies on
+ * mixed method on its all-pairs kernel; the sorted kernel (NB_FLAG_MIXED_SORTED,
+ * the default from 28,672 bodies) re-sorts the bodies on
  * load, which changes its summation order (results stay within tolerance). */
 nb_status nb_checkpoint_load(nb_sim *sim, const char *path);
 
