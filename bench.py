@@ -30,6 +30,11 @@ import sys
 import threading
 import time
 
+# The serving extra runs its Barnes-Hut jobs on 16 streams; the CUDA runtime
+# maps streams onto CUDA_DEVICE_MAX_CONNECTIONS hardware queues (8 by
+# default), so give it as many before CUDA starts (a per-process setting).
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 REPO = os.path.dirname(os.path.abspath(__file__))
 PKG_DIR = os.path.join(REPO, "n-body-gravity-simulation_gb300")
 sys.path.insert(0, PKG_DIR)

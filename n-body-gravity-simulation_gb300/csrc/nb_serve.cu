@@ -9,7 +9,9 @@
 //        together: one per-body kick-drift and kick over the pool and one
 //        persistent batched force launch over all of them (nb_batch.cu);
 //      - Barnes-Hut jobs each own a simulation object and run on one of
-//        kBHStreams streams, each stream's jobs issued by its own host thread
+//        kBHStreams streams (the process should allow that many hardware
+//        queues: CUDA_DEVICE_MAX_CONNECTIONS >= 16), each stream's jobs issued
+//        by its own host thread
 //        (a tree build reads its node count on the host, which then blocks
 //        only that stream's later jobs), overlapping with the direct batch and
 //        with each other;
@@ -40,7 +42,7 @@ using Clock = std::chrono::steady_clock;
 
 constexpr size_t kDirectBytesPerBody = 10 * 8 + 32;  // FP64 planes + hi/lo mirror
 constexpr size_t kBHBytesPerBody = 320;              // state + sort + tree buffers (upper bound)
-constexpr int kBHStreams = 8;
+constexpr int kBHStreams = 16;
 
 struct Job {
     int64_t id = 0;
