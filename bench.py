@@ -512,7 +512,9 @@ def run_serving(a, nb, np):
             "queue_ms_p50": st["queue_ms_p50"], "queue_ms_p99": st["queue_ms_p99"],
             "ginteractions_s": st["interactions"] / wall / 1e9,
             "device_busy_fraction": st["busy_ms"] / 1e3 / wall,
-            "max_running": st["max_running"], "peak_device_gb": st["peak_device_bytes"] / 1e9}
+            "max_running": st["max_running"], "peak_device_gb": st["peak_device_bytes"] / 1e9,
+            "host_s": {"admit": st["host_admit_ms"] / 1e3, "issue": st["host_issue_ms"] / 1e3,
+                       "wait": st["host_wait_ms"] / 1e3, "retire": st["host_retire_ms"] / 1e3}}
 
 
 # ---------------------------------------------------------------- our arm

@@ -305,6 +305,10 @@ typedef struct nb_server_stats {
     double queue_ms_p50, queue_ms_p99; /* submission -> admission (wall clock) */
     int max_running;
     size_t peak_device_bytes;
+    /* host wall time per tick phase, summed: admitting jobs (allocation and
+     * upload), issuing the step (Barnes-Hut threads joined), waiting for the
+     * device, retiring finished jobs (download and release) */
+    double host_admit_ms, host_issue_ms, host_wait_ms, host_retire_ms;
 } nb_server_stats;
 
 /* G 1, softening 1e-3, theta 0.6, leaf 8, direct below 16384 bodies, dt 1e-3,

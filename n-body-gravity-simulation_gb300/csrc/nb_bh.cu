@@ -600,13 +600,13 @@ __device__ __forceinline__ float box_ext2(float4 lo, float4 hi)
 
 // Monopoles of every node; bounding boxes and sides of the leaves.
 __global__ void __launch_bounds__(256)
-refit_kernel(BHNode *__restrict__ nodes, int num_nodes,
+refit_kernel(BHNode *__restrict__ nodes, const int *__restrict__ total,
              const unsigned char *__restrict__ node_depth, const D4 *__restrict__ P,
              const BHRoot *__restrict__ root, const float4 *__restrict__ body,
              float4 *__restrict__ boxes)
 {
     const int k = blockIdx.x * 256 + threadIdx.x;
-    if (k >= num_nodes) return;
+    if (k >= *total) return;
     BHNode nd = nodes[k];
     const D4 hi = P[nd.first + nd.count], lo = P[nd.first];
     const double mass = hi.x - lo.x;
@@ -631,12 +631,12 @@ refit_kernel(BHNode *__restrict__ nodes, int num_nodes,
 // Internal nodes of depth d: box = union of the children's boxes (children:
 // node + 1, then each child's skip pointer up to the node's own).
 __global__ void __launch_bounds__(256)
-refit_level_kernel(BHNode *__restrict__ nodes, int num_nodes,
+refit_level_kernel(BHNode *__restrict__ nodes, const int *__restrict__ total,
                    const unsigned char *__restrict__ node_depth, int d,
                    const BHRoot *__restrict__ root, float4 *__restrict__ boxes)
 {
     const int k = blockIdx.x * 256 + threadIdx.x;
-    if (k >= num_nodes || node_depth[k] != d) return;
+    if (k >= *total || node_depth[k] != d) return;
     const int skip = nodes[k].skip;
     if (skip == k + 1) return;  // leaf: done by refit_kernel
     float4 mn = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f);
@@ -657,11 +657,11 @@ refit_level_kernel(BHNode *__restrict__ nodes, int num_nodes,
 // relative to the root centre, c the centre of mass),
 // Q = 3 S - tr(S) I; stored as (Qxx, Qyy, Qzz, Qxy), (Qxz, Qyz, 0, 0).
 __global__ void __launch_bounds__(256)
-quad_kernel(const BHNode *__restrict__ nodes, int num_nodes, const D4 *__restrict__ P,
+quad_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total, const D4 *__restrict__ P,
             const D4 *__restrict__ PA, const D4 *__restrict__ PB, float4 *__restrict__ quad)
 {
     const int k = blockIdx.x * 256 + threadIdx.x;
-    if (k >= num_nodes) return;
+    if (k >= *total) return;
     const int a = nodes[k].first, b = a + nodes[k].count;
     const double M = P[b].x - P[a].x;
     float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
@@ -692,11 +692,13 @@ constexpr int kWalkBlock = 128;
 // of mass (softened |r| throughout).
 template <bool ZERO_SOFT, bool QUAD>
 __global__ void __launch_bounds__(kWalkBlock)
-walk_kernel(const BHNode *__restrict__ nodes, int num_nodes, const float4 *__restrict__ body,
-            const uint32_t *__restrict__ order, int n, float theta2, float eps2, double G,
-            double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
-            BHStats *__restrict__ stats, const float4 *__restrict__ quad)
+walk_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
+            const float4 *__restrict__ body, const uint32_t *__restrict__ order, int n,
+            float theta2, float eps2, double G, double *__restrict__ ax,
+            double *__restrict__ ay, double *__restrict__ az, BHStats *__restrict__ stats,
+            const float4 *__restrict__ quad)
 {
+    const int num_nodes = *total;
     const int lane = threadIdx.x & 31;
     const int warp0 = (blockIdx.x * kWalkBlock + threadIdx.x) - lane;
     if (warp0 >= n) return;  // whole warp past the end
@@ -796,11 +798,13 @@ walk_kernel(const BHNode *__restrict__ nodes, int num_nodes, const float4 *__res
 // never a coarser walk than any body's own.
 template <bool ZERO_SOFT, bool QUAD, int NP>
 __global__ void __launch_bounds__(kWalkBlock)
-walk2_kernel(const BHNode *__restrict__ nodes, int num_nodes, const float4 *__restrict__ body,
-             const uint32_t *__restrict__ order, int n, float theta2, float eps2, double G,
-             double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
-             BHStats *__restrict__ stats, const float4 *__restrict__ quad)
+walk2_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
+             const float4 *__restrict__ body, const uint32_t *__restrict__ order, int n,
+             float theta2, float eps2, double G, double *__restrict__ ax,
+             double *__restrict__ ay, double *__restrict__ az, BHStats *__restrict__ stats,
+             const float4 *__restrict__ quad)
 {
+    const int num_nodes = *total;
     constexpr int kPer = 64 * NP;  // bodies per warp
     const int lane = threadIdx.x & 31;
     const int w0 = ((blockIdx.x * kWalkBlock + threadIdx.x) >> 5) * kPer;
@@ -944,7 +948,10 @@ nb_status scan_exclusive(const T *in, int n, T *out, DevBuf &tmp, cudaStream_t s
 
 struct BHTree {
     int n = 0;
-    int num_nodes = 0;
+    int num_nodes = -1;         // host copy of the node count (-1: not read back yet)
+    int node_cap = 0;           // node slots reserved (an upper bound of the count)
+    int *h_total = nullptr;     // pinned host copy of the count, filled asynchronously
+    cudaEvent_t total_ready = nullptr;
     DevBuf part, root, keys0, keys1, vals0, vals1, hist, body, moments, prefix, chain_len,
         chain_depth, offsets, scan_tmp, nodes, node_depth, boxes, stats, moments2a, moments2b,
         prefix2a, prefix2b, quad;
@@ -960,6 +967,11 @@ void bh_invalidate(BHTree *t)
     if (t) t->tree_valid = false;
 }
 
+void bh_mark_count_stale(BHTree *t)
+{
+    if (t) t->num_nodes = -1;
+}
+
 BHTree *bh_create() { return new BHTree(); }
 
 void bh_destroy(BHTree *t)
@@ -971,7 +983,40 @@ void bh_destroy(BHTree *t)
                       &t->boxes, &t->stats, &t->moments2a, &t->moments2b, &t->prefix2a,
                       &t->prefix2b, &t->quad};
     for (DevBuf *b : bufs) b->release();
+    if (t->h_total) cudaFreeHost(t->h_total);
+    if (t->total_ready) cudaEventDestroy(t->total_ready);
     delete t;
+}
+
+// The device copy of the node count of the last build (scan total).
+static const int *d_total(const BHTree *t) { return t->offsets.as<int>() + t->n; }
+
+// Nodes to launch over: the count if it has been read back, else the bound.
+static int launch_nodes(const BHTree *t) { return t->num_nodes >= 0 ? t->num_nodes : t->node_cap; }
+
+// The node count on the host (waits for its asynchronous read-back).
+static nb_status known_nodes(BHTree *t, int *count)
+{
+    if (t->num_nodes < 0) {
+        NB_CUDA_TRY(cudaEventSynchronize(t->total_ready));
+        t->num_nodes = *t->h_total;
+    }
+    *count = t->num_nodes;
+    return NB_OK;
+}
+
+// An upper bound of the node count of n bodies: the cells of one depth that
+// split are disjoint and hold more than leaf_capacity bodies each (and there
+// are at most 8^d of them); every leaf holds a body.
+static size_t node_bound(int n, int leaf_capacity)
+{
+    const size_t per_level = (size_t)n / (size_t)(std::max(leaf_capacity, 0) + 1);
+    size_t total = (size_t)n, cells = 1;
+    for (int d = 0; d < kMaxLevels; ++d) {
+        total += std::min(cells, per_level);
+        cells = std::min(cells * 8, (size_t)1 << 40);
+    }
+    return total;
 }
 
 // Root cube, 63-bit codes and the stable LSD sort of the code bits
@@ -1054,15 +1099,15 @@ void walk_launch(BHTree *t, int n, float theta2, float eps2, double G, double *a
     const int np = walk_pairs();
     if (np == 2)
         walk2_kernel<ZS, Q, 2><<<div_up(n, 4 * kWalkBlock), kWalkBlock, 0, st>>>(
-            t->nodes.as<BHNode>(), t->num_nodes, t->body.as<float4>(), t->order, n, theta2,
+            t->nodes.as<BHNode>(), d_total(t), t->body.as<float4>(), t->order, n, theta2,
             eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>());
     else if (np == 1)
         walk2_kernel<ZS, Q, 1><<<div_up(n, 2 * kWalkBlock), kWalkBlock, 0, st>>>(
-            t->nodes.as<BHNode>(), t->num_nodes, t->body.as<float4>(), t->order, n, theta2,
+            t->nodes.as<BHNode>(), d_total(t), t->body.as<float4>(), t->order, n, theta2,
             eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>());
     else
         walk_kernel<ZS, Q><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
-            t->nodes.as<BHNode>(), t->num_nodes, t->body.as<float4>(), t->order, n, theta2,
+            t->nodes.as<BHNode>(), d_total(t), t->body.as<float4>(), t->order, n, theta2,
             eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>());
 }
 
@@ -1088,7 +1133,7 @@ static nb_status compute_quads(BHTree *t, const double *x, const double *y, cons
                                const double *m, int n, cudaStream_t st)
 {
     const size_t N = (size_t)n;
-    const int nn = t->num_nodes;
+    const int nn = launch_nodes(t);
     NB_TRY(t->moments2a.reserve(sizeof(D4) * N));
     NB_TRY(t->moments2b.reserve(sizeof(D4) * N));
     NB_TRY(t->prefix2a.reserve(sizeof(D4) * (N + 1)));
@@ -1100,7 +1145,7 @@ static nb_status compute_quads(BHTree *t, const double *x, const double *y, cons
     NB_LAUNCH_CHECK();
     NB_TRY(scan_exclusive<D4>(t->moments2a.as<D4>(), n, t->prefix2a.as<D4>(), t->scan_tmp, st));
     NB_TRY(scan_exclusive<D4>(t->moments2b.as<D4>(), n, t->prefix2b.as<D4>(), t->scan_tmp, st));
-    quad_kernel<<<div_up(nn, 256), 256, 0, st>>>(t->nodes.as<BHNode>(), nn, t->prefix.as<D4>(),
+    quad_kernel<<<div_up(nn, 256), 256, 0, st>>>(t->nodes.as<BHNode>(), d_total(t), t->prefix.as<D4>(),
                                                  t->prefix2a.as<D4>(), t->prefix2b.as<D4>(),
                                                  t->quad.as<float4>());
     NB_LAUNCH_CHECK();
@@ -1112,13 +1157,14 @@ static nb_status refit(BHTree *t, const double *x, const double *y, const double
                        const double *m, int n, cudaStream_t st)
 {
     const BHRoot *root = t->root.as<BHRoot>();
-    const int nn = t->num_nodes;
+    int nn = 0;
+    NB_TRY(known_nodes(t, &nn));  // read back during an earlier evaluation
     NB_TRY(t->boxes.reserve(sizeof(float4) * 2 * (size_t)nn));
     gather_kernel<<<div_up(n, 256), 256, 0, st>>>(t->order, x, y, z, m, n, root,
                                                   t->body.as<float4>(), t->moments.as<D4>());
     NB_LAUNCH_CHECK();
     NB_TRY(scan_exclusive<D4>(t->moments.as<D4>(), n, t->prefix.as<D4>(), t->scan_tmp, st));
-    refit_kernel<<<div_up(nn, 256), 256, 0, st>>>(t->nodes.as<BHNode>(), nn,
+    refit_kernel<<<div_up(nn, 256), 256, 0, st>>>(t->nodes.as<BHNode>(), d_total(t),
                                                   t->node_depth.as<unsigned char>(),
                                                   t->prefix.as<D4>(), root, t->body.as<float4>(),
                                                   t->boxes.as<float4>());
@@ -1127,7 +1173,7 @@ static nb_status refit(BHTree *t, const double *x, const double *y, const double
     // deepest possible level)
     for (int d = kMaxLevels - 1; d >= 0; --d) {
         refit_level_kernel<<<div_up(nn, 256), 256, 0, st>>>(
-            t->nodes.as<BHNode>(), nn, t->node_depth.as<unsigned char>(), d, root,
+            t->nodes.as<BHNode>(), d_total(t), t->node_depth.as<unsigned char>(), d, root,
             t->boxes.as<float4>());
         NB_LAUNCH_CHECK();
     }
@@ -1174,17 +1220,27 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     NB_LAUNCH_CHECK();
     NB_TRY(scan_exclusive<int>(t->chain_len.as<int>(), n, t->offsets.as<int>(), t->scan_tmp,
                                st));
-    int total = 0;
-    NB_CUDA_TRY(cudaMemcpyAsync(&total, t->offsets.as<int>() + n, sizeof(int),
+    // No host read of the node count before the walk: node storage is sized
+    // for the bound, the kernels read the count on the device, and the count
+    // comes back to the host asynchronously for later launches and queries.
+    const size_t cap = node_bound(n, leaf_capacity);
+    NB_TRY(t->nodes.reserve(sizeof(BHNode) * cap));
+    NB_TRY(t->node_depth.reserve(cap));
+    if (!t->h_total) NB_CUDA_TRY(cudaMallocHost(&t->h_total, sizeof(int)));
+    if (!t->total_ready) NB_CUDA_TRY(cudaEventCreateWithFlags(&t->total_ready,
+                                                              cudaEventDisableTiming));
+    NB_CUDA_TRY(cudaMemcpyAsync(t->h_total, t->offsets.as<int>() + n, sizeof(int),
                                 cudaMemcpyDeviceToHost, st));
-    NB_CUDA_TRY(cudaStreamSynchronize(st));
-    if (total <= 0) return fail(NB_ERR_DEVICE_FAULT, "Barnes-Hut: empty tree");
-    if ((size_t)total * sizeof(BHNode) > t->nodes.bytes) {
-        const size_t room = (size_t)total + total / 4 + 1024;
-        NB_TRY(t->nodes.reserve(sizeof(BHNode) * room));
-        NB_TRY(t->node_depth.reserve(room));
-    }
-    t->num_nodes = total;
+    // inside a captured step graph the record must be an external event node
+    // (recorded by every replay) for the host to be able to wait for the count
+    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+    NB_CUDA_TRY(cudaStreamIsCapturing(st, &capturing));
+    if (capturing == cudaStreamCaptureStatusActive)
+        NB_CUDA_TRY(cudaEventRecordWithFlags(t->total_ready, st, cudaEventRecordExternal));
+    else
+        NB_CUDA_TRY(cudaEventRecord(t->total_ready, st));
+    t->node_cap = (int)std::min(cap, (size_t)INT32_MAX);
+    t->num_nodes = -1;
     t->n = n;
     NB_CUDA_TRY(cudaMemsetAsync(stats, 0, sizeof(BHStats), st));
     node_kernel<<<div_up(n, 256), 256, 0, st>>>(kin, n, leaf_capacity, root,
@@ -1209,7 +1265,9 @@ nb_status bh_info(BHTree *t, cudaStream_t st, nb_bh_info *info)
     NB_CUDA_TRY(cudaMemcpyAsync(&r, t->root.ptr, sizeof(r), cudaMemcpyDeviceToHost, st));
     NB_CUDA_TRY(cudaMemcpyAsync(&s, t->stats.ptr, sizeof(s), cudaMemcpyDeviceToHost, st));
     NB_CUDA_TRY(cudaStreamSynchronize(st));
-    info->num_nodes = t->num_nodes;
+    int nn = 0;
+    NB_TRY(known_nodes(t, &nn));
+    info->num_nodes = nn;
     info->num_leaves = s.leaves;
     info->max_depth = s.max_depth;
     info->split_levels = r.levels;
@@ -1240,10 +1298,11 @@ nb_status bh_read_nodes(BHTree *t, cudaStream_t st, int max_nodes, int *depth,
                         float *com_mass)
 {
     if (!t->n) return fail(NB_ERR_NOT_LOADED, "no Barnes-Hut tree built");
-    if (max_nodes < t->num_nodes)
-        return fail(NB_ERR_CAPACITY, "max_nodes is smaller than the node count");
-    std::vector<BHNode> h(t->num_nodes);
-    std::vector<unsigned char> dep(t->num_nodes);
+    int nn = 0;
+    NB_TRY(known_nodes(t, &nn));
+    if (max_nodes < nn) return fail(NB_ERR_CAPACITY, "max_nodes is smaller than the node count");
+    std::vector<BHNode> h(nn);
+    std::vector<unsigned char> dep(nn);
     std::vector<uint64_t> codes(t->n);
     BHRoot r;
     NB_CUDA_TRY(cudaMemcpyAsync(h.data(), t->nodes.ptr, sizeof(BHNode) * h.size(),
@@ -1254,7 +1313,7 @@ nb_status bh_read_nodes(BHTree *t, cudaStream_t st, int max_nodes, int *depth,
                                 cudaMemcpyDeviceToHost, st));
     NB_CUDA_TRY(cudaMemcpyAsync(&r, t->root.ptr, sizeof(r), cudaMemcpyDeviceToHost, st));
     NB_CUDA_TRY(cudaStreamSynchronize(st));
-    for (int k = 0; k < t->num_nodes; ++k) {
+    for (int k = 0; k < nn; ++k) {
         const BHNode &nd = h[k];
         const int d = dep[k];
         if (depth) depth[k] = d;

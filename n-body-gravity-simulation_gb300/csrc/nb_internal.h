@@ -202,6 +202,8 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
                      const KernelTimer *timer = nullptr, int reuse = 1, bool quad = false);
 // The next bh_compute rebuilds (the bodies were replaced).
 void bh_invalidate(BHTree *t);
+// A replayed build changed the node count behind the host's back.
+void bh_mark_count_stale(BHTree *t);
 nb_status bh_info(BHTree *t, cudaStream_t st, nb_bh_info *info);
 // Morton order of the bodies by the top 3*levels code bits: *order maps a
 // sorted index to the original one; *root_centre points at the device copy of
@@ -237,6 +239,19 @@ struct nb_sim {
     nb::DevBuf diag_scratch;
     nb::BHTree *bh = nullptr;
 
+    // One step as a CUDA graph (nb_step): captured on the second of two
+    // consecutive eligible steps with the same integrator and dt, replayed
+    // while they and the accelerations-valid flag stay the same; any load,
+    // configuration or flag change drops it.
+    cudaGraphExec_t step_graph = nullptr;
+    int graph_integ = -1;
+    double graph_dt = 0.0;
+    bool graph_fv_before = false, graph_fv_after = false;  // forces_valid around the step
+    uint64_t graph_kernels = 0;     // kernel nodes per replay (launch accounting)
+    int warm_integ = -1;            // the last uncaptured eligible step
+    double warm_dt = 0.0;
+    bool graphs_off = false;        // a capture failed: run steps directly
+
     // Optional timing of the dominant force kernel (nb_profile_*).
     bool profiling = false;
     std::vector<nb::KernelTimer> timers;
@@ -258,4 +273,8 @@ namespace nb {
 // Evaluates accelerations of positions (px,py,pz) with masses m into out*.
 nb_status eval_forces(nb_sim *s, const double *px, const double *py, const double *pz,
                       double *oax, double *oay, double *oaz);
+// Drops the captured step graph (the next steps run directly).
+void reset_step_graph(nb_sim *s);
+// Kernel launches made by a graph replay (the launch counter's evidence).
+void count_launches(uint64_t k);
 }

@@ -144,6 +144,7 @@ struct nb_server {
     double interactions = 0.0, busy_ms = 0.0;
     uint64_t submitted = 0, steps_done = 0, ticks = 0;
     int max_running = 0;
+    double admit_ms = 0.0, issue_ms = 0.0, wait_ms = 0.0, retire_ms = 0.0;
 };
 
 namespace nb {
@@ -259,10 +260,18 @@ nb_status retire(nb_server *s)
     return NB_OK;
 }
 
+double ms_since(Clock::time_point t0)
+{
+    return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
 nb_status tick(nb_server *s)
 {
     std::vector<Job *> new_direct;
+    auto t_phase = Clock::now();
     NB_TRY(admit(s, new_direct));
+    s->admit_ms += ms_since(t_phase);
+    t_phase = Clock::now();
     if (s->running.empty()) return NB_OK;
     s->max_running = std::max(s->max_running, (int)s->running.size());
     std::vector<Job *> direct, bh;
@@ -339,8 +348,11 @@ nb_status tick(nb_server *s)
     for (auto &t : workers) t.join();
     for (int k = 0; k < kBHStreams; ++k)
         if (bh_status[k] != NB_OK) return fail(bh_status[k], bh_error[k]);
+    s->issue_ms += ms_since(t_phase);
+    t_phase = Clock::now();
     NB_CUDA_TRY(cudaStreamSynchronize(s->stream));
     for (int k = 0; k < kBHStreams; ++k) NB_CUDA_TRY(cudaStreamSynchronize(s->bh_streams[k]));
+    s->wait_ms += ms_since(t_phase);
     float tick_ms = 0.f;
     if (!direct.empty()) {
         NB_CUDA_TRY(cudaEventElapsedTime(&tick_ms, s->tick_start, s->direct_done));
@@ -363,7 +375,10 @@ nb_status tick(nb_server *s)
     s->busy_ms += tick_ms;
     s->steps_done += direct.size() + bh.size();
     ++s->ticks;
-    return retire(s);
+    t_phase = Clock::now();
+    const nb_status r = retire(s);
+    s->retire_ms += ms_since(t_phase);
+    return r;
 }
 
 } // namespace
@@ -519,6 +534,10 @@ nb_status nb_server_get_stats(nb_server *s, nb_server_stats *out)
     out->queue_ms_p99 = quantile(s->queue_ms, 0.99);
     out->max_running = s->max_running;
     out->peak_device_bytes = s->peak_bytes;
+    out->host_admit_ms = s->admit_ms;
+    out->host_issue_ms = s->issue_ms;
+    out->host_wait_ms = s->wait_ms;
+    out->host_retire_ms = s->retire_ms;
     return NB_OK;
 }
 

@@ -42,6 +42,7 @@ const KernelTimer *next_timer(nb_sim *s)
 } // namespace
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(uint64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
 void set_error(const std::string &msg) { g_last_error = msg; }
 
@@ -209,6 +210,92 @@ static nb_status step_once(nb_sim *s, int integ, double dt)
     }
 }
 
+void reset_step_graph(nb_sim *s)
+{
+    if (s->step_graph) cudaGraphExecDestroy(s->step_graph);
+    s->step_graph = nullptr;
+    s->graph_integ = -1;
+    s->warm_integ = -1;
+}
+
+// Steps whose launch sequence is the same every time (no host-side choice
+// that depends on earlier evaluations: not the re-sorting mixed kernel, not
+// Barnes-Hut tree reuse), on a stream that may be captured.
+static bool graph_eligible(const nb_sim *s)
+{
+    if (s->graphs_off || s->profiling || s->stream == nullptr) return false;
+    switch (s->cfg.method) {
+    case NB_DIRECT_FP64: return true;
+    case NB_DIRECT_MIXED: return !direct_sorted_enabled((int)s->n, s->cfg.flags);
+    case NB_BARNES_HUT: return NB_FLAG_BH_REUSE_OF(s->cfg.flags) <= 1;
+    default: return false;
+    }
+}
+
+// Captures one step into a graph and launches it.  A failed capture (a call
+// that cannot be captured) turns graphs off for this simulation and runs the
+// step directly.
+static nb_status capture_step(nb_sim *s, int integ, double dt)
+{
+    reset_step_graph(s);
+    const bool fv = s->forces_valid;
+    NB_CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    const nb_status r = step_once(s, integ, dt);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    if (r != NB_OK) {
+        if (g) cudaGraphDestroy(g);
+        return r;
+    }
+    cudaGraphExec_t exec = nullptr;
+    if (e == cudaSuccess && g && cudaGraphInstantiate(&exec, g, 0) == cudaSuccess) {
+        size_t count = 0;
+        cudaGraphGetNodes(g, nullptr, &count);
+        std::vector<cudaGraphNode_t> nodes(count);
+        if (count) cudaGraphGetNodes(g, nodes.data(), &count);
+        uint64_t kernels = 0;
+        for (auto nd : nodes) {
+            cudaGraphNodeType type;
+            if (cudaGraphNodeGetType(nd, &type) == cudaSuccess && type == cudaGraphNodeTypeKernel)
+                ++kernels;
+        }
+        cudaGraphDestroy(g);
+        s->step_graph = exec;
+        s->graph_integ = integ;
+        s->graph_dt = dt;
+        s->graph_fv_before = fv;
+        s->graph_fv_after = s->forces_valid;
+        s->graph_kernels = kernels;
+        NB_CUDA_TRY(cudaGraphLaunch(exec, s->stream));
+        return NB_OK;
+    }
+    // capture did not produce a graph: nothing ran; run the step directly
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    s->graphs_off = true;
+    s->forces_valid = fv;
+    return step_once(s, integ, dt);
+}
+
+static nb_status step_with_graphs(nb_sim *s, int integ, double dt)
+{
+    if (!graph_eligible(s)) return step_once(s, integ, dt);
+    if (s->step_graph && s->graph_integ == integ && s->graph_dt == dt &&
+        s->graph_fv_before == s->forces_valid) {
+        NB_CUDA_TRY(cudaGraphLaunch(s->step_graph, s->stream));
+        count_launches(s->graph_kernels);
+        s->forces_valid = s->graph_fv_after;
+        if (s->cfg.method == NB_BARNES_HUT) bh_mark_count_stale(s->bh);
+        return NB_OK;
+    }
+    if (s->warm_integ == integ && s->warm_dt == dt) return capture_step(s, integ, dt);
+    reset_step_graph(s);
+    NB_TRY(step_once(s, integ, dt));
+    s->warm_integ = integ;
+    s->warm_dt = dt;
+    return NB_OK;
+}
+
 } // namespace nb
 
 using namespace nb;
@@ -263,6 +350,7 @@ nb_status nb_destroy(nb_sim *s)
 {
     if (!s) return NB_OK;
     cudaStreamSynchronize(s->stream);
+    reset_step_graph(s);
     for (auto &t : s->timers) {
         cudaEventDestroy(t.start);
         cudaEventDestroy(t.stop);
@@ -287,7 +375,9 @@ nb_status nb_set_config(nb_sim *s, const nb_config *cfg)
     const bool same = s->cfg.method == cfg->method && s->cfg.G == cfg->G &&
                       s->cfg.softening == cfg->softening && s->cfg.theta == cfg->theta &&
                       s->cfg.leaf_capacity == cfg->leaf_capacity;
+    const bool flags_changed = s->cfg.flags != cfg->flags;
     s->cfg = *cfg;
+    if (!same || flags_changed) reset_step_graph(s);
     if (!same) {
         s->forces_valid = false;
         bh_invalidate(s->bh);
@@ -319,6 +409,7 @@ static nb_status load_impl(nb_sim *s, size_t n, const double *const *src, cudaMe
     s->forces_valid = false;
     s->sorted.invalidate_order();
     bh_invalidate(s->bh);
+    reset_step_graph(s);
     return NB_OK;
 }
 
@@ -373,6 +464,7 @@ nb_status nb_bind_device(nb_sim *s, size_t n, double *const *arrays10)
         s->forces_valid = false;
         s->sorted.invalidate_order();
         bh_invalidate(s->bh);
+        reset_step_graph(s);
     }
     return NB_OK;
 }
@@ -407,7 +499,7 @@ nb_status nb_step(nb_sim *s, int integrator, double dt, int nsteps)
     if (integrator < NB_EULER || integrator > NB_RK4)
         return fail(NB_ERR_INVALID_ARGUMENT, "unknown integrator");
     if (s->n == 0) return fail(NB_ERR_NOT_LOADED, "no bodies loaded");
-    for (int k = 0; k < nsteps; ++k) NB_TRY(step_once(s, integrator, dt));
+    for (int k = 0; k < nsteps; ++k) NB_TRY(step_with_graphs(s, integrator, dt));
     return NB_OK;
 }
 
@@ -474,6 +566,7 @@ nb_status nb_profile_enable(nb_sim *s, int enable)
 {
     if (!s) return fail(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
     s->profiling = enable != 0;
+    reset_step_graph(s);
     return NB_OK;
 }
 

@@ -105,7 +105,9 @@ class _ServerStats(C.Structure):
                 ("interactions", C.c_double), ("busy_ms", C.c_double),
                 ("step_ms_p50", C.c_double), ("step_ms_p99", C.c_double),
                 ("queue_ms_p50", C.c_double), ("queue_ms_p99", C.c_double),
-                ("max_running", C.c_int), ("peak_device_bytes", C.c_size_t)]
+                ("max_running", C.c_int), ("peak_device_bytes", C.c_size_t),
+                ("host_admit_ms", C.c_double), ("host_issue_ms", C.c_double),
+                ("host_wait_ms", C.c_double), ("host_retire_ms", C.c_double)]
 
 
 def kernel_launch_count() -> int:
