@@ -5,7 +5,7 @@ import os
 import numpy as np
 import pytest
 
-REF_PARTICLES = "/root/reference/particles_100.txt"
+REF_PARTICLES = os.path.join(os.environ.get("REF_ROOT", "/root/reference"), "particles_100.txt")
 
 
 def test_particles_round_trip_bit_exact(nb, tmp_path):
