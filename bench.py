@@ -514,7 +514,11 @@ def run_serving(a, nb, np):
             "device_busy_fraction": st["busy_ms"] / 1e3 / wall,
             "max_running": st["max_running"], "peak_device_gb": st["peak_device_bytes"] / 1e9,
             "host_s": {"admit": st["host_admit_ms"] / 1e3, "issue": st["host_issue_ms"] / 1e3,
-                       "wait": st["host_wait_ms"] / 1e3, "retire": st["host_retire_ms"] / 1e3}}
+                       "wait": st["host_wait_ms"] / 1e3, "retire": st["host_retire_ms"] / 1e3,
+                       "issue_upload": st["host_upload_ms"] / 1e3,
+                       "issue_direct": st["host_direct_ms"] / 1e3,
+                       "issue_join": st["host_join_ms"] / 1e3},
+            "ticks": st["ticks"]}
 
 
 # ---------------------------------------------------------------- our arm

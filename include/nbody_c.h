@@ -206,6 +206,7 @@ typedef struct nb_bh_info {
     double root[4];     /* centre x, y, z and side of the root cube */
     uint64_t interactions_m2p;  /* body-node (monopole) terms of the last walk */
     uint64_t interactions_p2p;  /* body-body terms of the last walk (self included) */
+    uint64_t interactions_total; /* all terms of every walk of this simulation */
 } nb_bh_info;
 
 /* Builds the tree of the current positions (without a walk) and reports it. */
@@ -309,6 +310,9 @@ typedef struct nb_server_stats {
      * upload), issuing the step (Barnes-Hut threads joined), waiting for the
      * device, retiring finished jobs (download and release) */
     double host_admit_ms, host_issue_ms, host_wait_ms, host_retire_ms;
+    /* parts of host_issue_ms: rebuilding the direct work queue, issuing the
+     * direct batch, waiting for the Barnes-Hut stream threads */
+    double host_upload_ms, host_direct_ms, host_join_ms;
 } nb_server_stats;
 
 /* G 1, softening 1e-3, theta 0.6, leaf 8, direct below 16384 bodies, dt 1e-3,

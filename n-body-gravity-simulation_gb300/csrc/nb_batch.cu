@@ -151,18 +151,20 @@ int bucket_of(int n)
 
 void build_work_items(const std::vector<SysDesc> &sys, std::vector<WorkItem> &items)
 {
+    // largest cost first: an item costs ~ n_j * 32 ipt, the same for every
+    // full item of a system, so the systems are ordered (stably) by that cost
+    // and each contributes its items in order -- O(items), no per-item sort
+    std::vector<int> by_cost(sys.size());
+    for (int s = 0; s < (int)sys.size(); ++s) by_cost[s] = s;
+    std::stable_sort(by_cost.begin(), by_cost.end(), [&](int a, int b) {
+        return (long)sys[a].n * std::min(32 * sys[a].ipt, sys[a].n) >
+               (long)sys[b].n * std::min(32 * sys[b].ipt, sys[b].n);
+    });
     items.clear();
-    for (int s = 0; s < (int)sys.size(); ++s) {
+    for (int s : by_cost) {
         const int per = 32 * sys[s].ipt;
         for (int i0 = 0; i0 < sys[s].n; i0 += per) items.push_back(WorkItem{s, i0});
     }
-    // largest cost first: cost ~ n_j * (bodies in the item)
-    std::stable_sort(items.begin(), items.end(), [&](const WorkItem &a, const WorkItem &b) {
-        const SysDesc &sa = sys[a.sys], &sb = sys[b.sys];
-        const long ca = (long)sa.n * std::min(32 * sa.ipt, sa.n - a.i0);
-        const long cb = (long)sb.n * std::min(32 * sb.ipt, sb.n - b.i0);
-        return ca > cb;
-    });
 }
 
 nb_status batch_forces(const float4 *hi, const float4 *lo, const SysDesc *d_sys,

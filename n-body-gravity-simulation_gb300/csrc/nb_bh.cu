@@ -43,6 +43,7 @@
 #include "nb_pair.cuh"
 
 #include <algorithm>
+#include <cstddef>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -81,8 +82,9 @@ struct alignas(32) BHNode {
 static_assert(sizeof(BHNode) == 32, "node layout");
 
 struct BHStats {
-    unsigned long long m2p, p2p;
+    unsigned long long m2p, p2p;  // terms of the last walk (reset by every build/refit)
     int leaves, max_depth;
+    unsigned long long total;     // terms of every walk of this tree object (never reset)
 };
 
 // ------------------------------------------------------------ bounding box
@@ -788,6 +790,7 @@ walk_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
     if (lane == 0) {
         atomicAdd(&stats->m2p, (unsigned long long)m2p * nv);
         atomicAdd(&stats->p2p, (unsigned long long)p2p * nv);
+        atomicAdd(&stats->total, (unsigned long long)(m2p + p2p) * nv);
     }
 }
 
@@ -924,6 +927,7 @@ walk2_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
     if (lane == 0) {
         atomicAdd(&stats->m2p, (unsigned long long)m2p * nv);
         atomicAdd(&stats->p2p, (unsigned long long)p2p * nv);
+        atomicAdd(&stats->total, (unsigned long long)(m2p + p2p) * nv);
     }
 }
 
@@ -1203,7 +1207,10 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     NB_TRY(t->chain_len.reserve(sizeof(int) * N));
     NB_TRY(t->chain_depth.reserve(sizeof(int) * N));
     NB_TRY(t->offsets.reserve(sizeof(int) * (N + 1)));
-    NB_TRY(t->stats.reserve(sizeof(BHStats)));
+    if (!t->stats.ptr) {
+        NB_TRY(t->stats.reserve(sizeof(BHStats)));
+        NB_CUDA_TRY(cudaMemsetAsync(t->stats.ptr, 0, sizeof(BHStats), st));
+    }
     NB_TRY(morton_sort(t, x, y, z, n, 0, st));
     BHRoot *root = t->root.as<BHRoot>();
     BHStats *stats = t->stats.as<BHStats>();
@@ -1242,7 +1249,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     t->node_cap = (int)std::min(cap, (size_t)INT32_MAX);
     t->num_nodes = -1;
     t->n = n;
-    NB_CUDA_TRY(cudaMemsetAsync(stats, 0, sizeof(BHStats), st));
+    NB_CUDA_TRY(cudaMemsetAsync(stats, 0, offsetof(BHStats, total), st));
     node_kernel<<<div_up(n, 256), 256, 0, st>>>(kin, n, leaf_capacity, root,
                                                 t->chain_len.as<int>(), t->chain_depth.as<int>(),
                                                 t->offsets.as<int>(), t->prefix.as<D4>(),
@@ -1277,6 +1284,7 @@ nb_status bh_info(BHTree *t, cudaStream_t st, nb_bh_info *info)
     info->root[3] = r.size;
     info->interactions_m2p = s.m2p;
     info->interactions_p2p = s.p2p;
+    info->interactions_total = s.total;
     return NB_OK;
 }
 

@@ -145,6 +145,7 @@ struct nb_server {
     uint64_t submitted = 0, steps_done = 0, ticks = 0;
     int max_running = 0;
     double admit_ms = 0.0, issue_ms = 0.0, wait_ms = 0.0, retire_ms = 0.0;
+    double upload_ms = 0.0, direct_ms = 0.0, join_ms = 0.0;  // parts of issue_ms
 };
 
 namespace nb {
@@ -246,6 +247,9 @@ nb_status retire(nb_server *s)
         } else {
             NB_TRY(nb_read_state(j->sim, r, r + n, r + 2 * n, r + 3 * n, r + 4 * n, r + 5 * n,
                                  r + 6 * n, r + 7 * n, r + 8 * n, r + 9 * n));
+            nb_bh_info info;
+            if (nb_bh_get_info(j->sim, &info) == NB_OK)
+                s->interactions += (double)info.interactions_total;
             nb_destroy(j->sim);
             j->sim = nullptr;
             s->bh_bytes -= kBHBytesPerBody * n;
@@ -280,8 +284,10 @@ nb_status tick(nb_server *s)
     const double dt = s->cfg.dt;
     const int hw = (int)s->slots.high_water;
     if (s->items_dirty) {
+        const auto t_up = Clock::now();
         NB_TRY(upload_systems(s, direct, s->d_sys, s->d_items, &s->num_items));
         s->items_dirty = false;
+        s->upload_ms += ms_since(t_up);
     }
     NB_CUDA_TRY(cudaEventRecord(s->tick_start, s->stream));
     // BH streams wait for the tick start so that latencies share one origin
@@ -323,6 +329,7 @@ nb_status tick(nb_server *s)
                 if (t.joinable()) t.join();
         }
     } joiner{workers};
+    const auto t_direct = Clock::now();
     if (!direct.empty()) {
         float4 *hi = s->hi.as<float4>(), *lo = s->lo.as<float4>();
         if (!new_direct.empty()) {
@@ -345,7 +352,10 @@ nb_status tick(nb_server *s)
                     nullptr, nullptr, nullptr, s->stream));
         NB_CUDA_TRY(cudaEventRecord(s->direct_done, s->stream));
     }
+    s->direct_ms += ms_since(t_direct);
+    const auto t_join = Clock::now();
     for (auto &t : workers) t.join();
+    s->join_ms += ms_since(t_join);
     for (int k = 0; k < kBHStreams; ++k)
         if (bh_status[k] != NB_OK) return fail(bh_status[k], bh_error[k]);
     s->issue_ms += ms_since(t_phase);
@@ -367,10 +377,7 @@ nb_status tick(nb_server *s)
         NB_CUDA_TRY(cudaEventElapsedTime(&ms, s->tick_start, j->step_done));
         tick_ms = std::max(tick_ms, ms);
         s->step_ms.push_back(ms);
-        nb_bh_info info;
-        NB_TRY(nb_bh_get_info(j->sim, &info));
-        s->interactions += (double)(info.interactions_m2p + info.interactions_p2p);
-        ++j->done;
+        ++j->done;  // its interactions are read once, at retirement
     }
     s->busy_ms += tick_ms;
     s->steps_done += direct.size() + bh.size();
@@ -538,6 +545,9 @@ nb_status nb_server_get_stats(nb_server *s, nb_server_stats *out)
     out->host_issue_ms = s->issue_ms;
     out->host_wait_ms = s->wait_ms;
     out->host_retire_ms = s->retire_ms;
+    out->host_upload_ms = s->upload_ms;
+    out->host_direct_ms = s->direct_ms;
+    out->host_join_ms = s->join_ms;
     return NB_OK;
 }
 

@@ -76,7 +76,8 @@ class _Diag(C.Structure):
 class _BHInfo(C.Structure):
     _fields_ = [("num_nodes", C.c_int), ("num_leaves", C.c_int), ("max_depth", C.c_int),
                 ("split_levels", C.c_int), ("root", C.c_double * 4),
-                ("interactions_m2p", C.c_uint64), ("interactions_p2p", C.c_uint64)]
+                ("interactions_m2p", C.c_uint64), ("interactions_p2p", C.c_uint64),
+                ("interactions_total", C.c_uint64)]
 
 
 class _Profile(C.Structure):
@@ -107,7 +108,9 @@ class _ServerStats(C.Structure):
                 ("queue_ms_p50", C.c_double), ("queue_ms_p99", C.c_double),
                 ("max_running", C.c_int), ("peak_device_bytes", C.c_size_t),
                 ("host_admit_ms", C.c_double), ("host_issue_ms", C.c_double),
-                ("host_wait_ms", C.c_double), ("host_retire_ms", C.c_double)]
+                ("host_wait_ms", C.c_double), ("host_retire_ms", C.c_double),
+                ("host_upload_ms", C.c_double), ("host_direct_ms", C.c_double),
+                ("host_join_ms", C.c_double)]
 
 
 def kernel_launch_count() -> int:
