@@ -393,8 +393,9 @@ nb_status nb_checkpoint_save(nb_sim *sim, const char *path);
  * simulation's capacity.  Continuing after a restore gives the same bits as
  * continuing the saved run for the FP64 and Barnes-Hut methods and for the
  * mixed method on its all-pairs kernel; the sorted kernel (NB_FLAG_MIXED_SORTED,
- * the default from 28,672 bodies) re-sorts the bodies on
- * load, which changes its summation order (results stay within tolerance). */
+ * the default from 28,672 bodies) sums in the order of its last Morton sort,
+ * which a restore into another simulation does not carry over (results stay
+ * within tolerance). */
 nb_status nb_checkpoint_load(nb_sim *sim, const char *path);
 
 /* ---- all-pairs forces without device allocation ----------------------------- */

@@ -94,8 +94,10 @@ struct SortedBuffers {
     DevBuf hi, lo, partials, boxes;
     BHTree *sorter = nullptr;
     // The Morton order is a performance device only (near/far decisions use
-    // the current chunk boxes), so it is recomputed every kResortEvals force
-    // evaluations, when n changes and after every load, not at every call.
+    // the current chunk boxes, any order gives results within tolerance), so
+    // it is recomputed every kResortEvals force evaluations and when n
+    // changes -- not at every call, and not on a load (the next periodic
+    // re-sort adapts it to bodies that moved or were replaced).
     const uint32_t *order = nullptr;  // sorted index -> body (sorter-owned)
     const double *centre = nullptr;   // origin of the hi/lo split (sorter-owned)
     int order_n = -1;

@@ -254,7 +254,6 @@ nb_status nb_checkpoint_load(nb_sim *s, const char *path)
     NB_CUDA_TRY(cudaStreamSynchronize(s->stream));
     s->n = n;
     s->forces_valid = valid != 0;
-    s->sorted.invalidate_order();
     nb::bh_invalidate(s->bh);
     nb::reset_step_graph(s);
     return NB_OK;

@@ -407,7 +407,6 @@ static nb_status load_impl(nb_sim *s, size_t n, const double *const *src, cudaMe
         NB_CUDA_TRY(cudaMemsetAsync(s->f[k], 0, bytes, s->stream));
     s->n = n;
     s->forces_valid = false;
-    s->sorted.invalidate_order();
     bh_invalidate(s->bh);
     reset_step_graph(s);
     return NB_OK;
@@ -462,7 +461,6 @@ nb_status nb_bind_device(nb_sim *s, size_t n, double *const *arrays10)
     s->n = n;
     if (!same) {
         s->forces_valid = false;
-        s->sorted.invalidate_order();
         bh_invalidate(s->bh);
         reset_step_graph(s);
     }
