@@ -610,7 +610,7 @@ def run_ours(a, rank, world, local_rank):
     peak = fp32_roofline_gint(props.multi_processor_count, peaks.get("sm_max_mhz", 2070.0))
     roofline = {
         "bound": "fp32",
-        "kernel": "direct_sorted_kernel" if n >= 28672 else "direct_mixed_kernel",
+        "kernel": "direct_sorted_kernel" if n >= 16384 else "direct_mixed_kernel",
         "achieved": achieved,
         "peak": peak, "unit": "Ginteractions/s", "frac": achieved / peak,
         "peak_basis": (f"{props.multi_processor_count} SMs x {peaks.get('sm_max_mhz', 2070.0)}"

@@ -98,8 +98,8 @@ typedef struct nb_config {
  * second moments).  The opening test is unchanged, so at the same theta the
  * force error drops (the reference is monopole-only). */
 #define NB_FLAG_BH_QUADRUPOLE 2
-/* NB_DIRECT_MIXED kernel choice.  By default systems of at least 28,672 bodies
- * take the Morton-sorted near/far kernel (far j-chunks in plain FP32 relative to
+/* NB_DIRECT_MIXED kernel choice.  By default systems of at least 16,384 bodies
+ * take the Hilbert-sorted near/far kernel (far j-chunks in plain FP32 relative to
  * a warp-local origin) and smaller ones the all-pairs double-single kernel;
  * these flags force one or the other (same accuracy criteria either way). */
 #define NB_FLAG_MIXED_SORTED 4
@@ -393,7 +393,7 @@ nb_status nb_checkpoint_save(nb_sim *sim, const char *path);
  * simulation's capacity.  Continuing after a restore gives the same bits as
  * continuing the saved run for the FP64 and Barnes-Hut methods and for the
  * mixed method on its all-pairs kernel; the sorted kernel (NB_FLAG_MIXED_SORTED,
- * the default from 28,672 bodies) sums in the order of its last Morton sort,
+ * the default from 16,384 bodies) sums in the order of its last Hilbert sort,
  * which a restore into another simulation does not carry over (results stay
  * within tolerance). */
 nb_status nb_checkpoint_load(nb_sim *sim, const char *path);

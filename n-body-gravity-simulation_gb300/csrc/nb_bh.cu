@@ -254,6 +254,62 @@ encode_kernel(const double *__restrict__ x, const double *__restrict__ y,
     vals[i] = (uint32_t)i;
 }
 
+// ------------------------------------------------------------ Hilbert encode
+// Position on the Hilbert curve through the 2^10 x 2^10 x 2^10 grid of the root
+// cube, following J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc.
+// 707 (2004): the grid coordinates are turned into the curve's "transposed"
+// index by reflections and exchanges from the top bit down, Gray-decoded, and
+// their bits interleaved (axis 0 most significant).  Consecutive indices are
+// face-adjacent cells, so a run of sorted bodies fills a compact region (the
+// Morton curve jumps between distant cells at every level boundary).
+__device__ __forceinline__ uint32_t hilbert_index30(uint32_t a0, uint32_t a1, uint32_t a2)
+{
+    uint32_t X[3] = {a0, a1, a2};
+    for (uint32_t q = 1u << 9; q > 1; q >>= 1) {
+        const uint32_t p = q - 1;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (X[i] & q) {
+                X[0] ^= p;  // reflect the low bits of axis 0
+            } else {        // exchange the low bits of axes 0 and i
+                const uint32_t t = (X[0] ^ X[i]) & p;
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0];
+    X[2] ^= X[1];
+    uint32_t t = 0;
+    for (uint32_t q = 1u << 9; q > 1; q >>= 1)
+        if (X[2] & q) t ^= q - 1;
+    X[0] ^= t;
+    X[1] ^= t;
+    X[2] ^= t;
+    return (uint32_t)((spread21(X[0]) << 2) | (spread21(X[1]) << 1) | spread21(X[2]));
+}
+
+// keys[i] = the 30-bit Hilbert index of body i in bits 33..62 (the bits a
+// 10-level Morton sort orders by), vals[i] = i.
+__global__ void __launch_bounds__(256)
+hilbert_kernel(const double *__restrict__ x, const double *__restrict__ y,
+               const double *__restrict__ z, int n, const BHRoot *__restrict__ root,
+               uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
+{
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= n) return;
+    const double size = root->size, scale = 1024.0 / size;
+    const double p[3] = {x[i], y[i], z[i]}, c[3] = {root->cx, root->cy, root->cz};
+    uint32_t g[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double f = floor((p[k] - (c[k] - size / 2)) * scale);
+        g[k] = (uint32_t)fmin(fmax(f, 0.0), 1023.0);
+    }
+    keys[i] = (uint64_t)hilbert_index30(g[0], g[1], g[2]) << 33;
+    vals[i] = (uint32_t)i;
+}
+
 // ------------------------------------------------------------ radix sort
 constexpr int kSortWarps = 8;
 constexpr int kSortRounds = 8;
@@ -1027,7 +1083,7 @@ static size_t node_bound(int n, int leaf_capacity)
 // [first_shift, 64) (first_shift 0: the full code).  Leaves the sorted codes
 // and the permutation (sorted index -> original index) in t.
 static nb_status morton_sort(BHTree *t, const double *x, const double *y, const double *z,
-                             int n, int first_shift, cudaStream_t st)
+                             int n, int first_shift, cudaStream_t st, bool hilbert = false)
 {
     const size_t N = (size_t)n;
     const int nparts = std::min(div_up(n, 256), 2 * device_props().num_sms);
@@ -1046,8 +1102,13 @@ static nb_status morton_sort(BHTree *t, const double *x, const double *y, const 
     NB_LAUNCH_CHECK();
     bbox_final_kernel<<<1, 256, 0, st>>>(t->part.as<double>(), nparts, root);
     NB_LAUNCH_CHECK();
-    encode_kernel<<<div_up(n, 256), 256, 0, st>>>(x, y, z, n, root, t->keys0.as<uint64_t>(),
-                                                   t->vals0.as<uint32_t>());
+    if (hilbert)
+        hilbert_kernel<<<div_up(n, 256), 256, 0, st>>>(x, y, z, n, root, t->keys0.as<uint64_t>(),
+                                                        t->vals0.as<uint32_t>());
+    else
+        encode_kernel<<<div_up(n, 256), 256, 0, st>>>(x, y, z, n, root,
+                                                       t->keys0.as<uint64_t>(),
+                                                       t->vals0.as<uint32_t>());
     NB_LAUNCH_CHECK();
 
     uint64_t *kin = t->keys0.as<uint64_t>(), *kout = t->keys1.as<uint64_t>();
@@ -1081,6 +1142,18 @@ nb_status bh_morton_order(BHTree *t, const double *x, const double *y, const dou
     NB_TRY(morton_sort(t, x, y, z, n, first_shift, st));
     *order = t->order;
     *root_centre = &t->root.as<BHRoot>()->cx;
+    t->tree_valid = false;  // the sort replaced the tree's codes
+    return NB_OK;
+}
+
+nb_status bh_hilbert_order(BHTree *t, const double *x, const double *y, const double *z, int n,
+                           cudaStream_t st, const uint32_t **order, const double **root_centre)
+{
+    if (n <= 0) return NB_OK;
+    NB_TRY(morton_sort(t, x, y, z, n, 32, st, true));  // key bits 32..63
+    *order = t->order;
+    *root_centre = &t->root.as<BHRoot>()->cx;
+    t->tree_valid = false;
     return NB_OK;
 }
 

@@ -1,18 +1,21 @@
-// nb_direct_sorted.cu -- the mixed-precision all-pairs sum over Morton-sorted
+// nb_direct_sorted.cu -- the mixed-precision all-pairs sum over Hilbert-sorted
 // bodies with a near/far split decided per warp and per 32-body j-chunk, in
 // packed FP32x2 arithmetic.
 //
 // Near/far.  The double-single displacement of the mixed pair term costs 6 of
 // its 21 FP32 operations and is needed only when a pair is close compared with
 // the distance of its bodies from the coordinate origin.  Here the origin
-// moves to each warp: bodies are sorted along a Morton curve (the Barnes-Hut
-// encode and radix sort), so the 32*IPT consecutive bodies a warp owns are
-// spatially compact.  The warp takes the centre c of their bounding box as
+// moves to each warp: bodies are sorted along a Hilbert curve (the Barnes-Hut
+// radix sort on Hilbert keys), so the 32*IPT consecutive bodies a warp owns are
+// spatially compact.  The Hilbert curve never jumps between distant cells (the
+// Morton curve does at every cell boundary), so its warp and chunk boxes are
+// smaller: on a 65,536-body Plummer sphere 5 % of the chunk pairs are near
+// instead of 11 %, and the kernel runs 4.7 % faster.  The warp takes the centre c of their bounding box as
 // origin and stages every j-chunk (32 consecutive sorted bodies, one per lane)
 // as a normalised double-single (S, E) of x - c.  A chunk whose bounding box
 // lies at least kFarFactor * D from the warp's box (D: the warp box diameter)
 // runs the plain FP32 term on S alone (15 FP32 operations + 1 MUFU), and a
-// chunk at least D/2 away drops the folded Newton step too (12 + 1); other
+// chunk at least kVeryFar * D away drops the folded Newton step too (12 + 1); other
 // chunks take the full double-single term on S and E (21 + 1).  Decisions are
 // uniform over the warp (no divergence) and a warp stages its own chunks in its
 // own shared memory: no CTA-wide barrier.
@@ -29,17 +32,18 @@
 // Error of a far term: S carries one FP32 rounding of x - c.  With
 // |xi - c| <= D/2, |xj - c| <= r + D/2 and the subtraction's own rounding, the
 // displacement error is at most 2^-24 (2r + D) <= 2^-24 r (2 + 1/kFarFactor)
-// = 6 * 2^-24 r for kFarFactor = 1/4 -- about 3.6e-7 relative at worst, the
-// order of the FP32 arithmetic of the term (measured on a 65,536-body Plummer
-// sphere, factors 1/2, 1/4 and 1/8 leave the RMS force error at 3.2e-8).  A
-// very far term (gap >= D/2: displacement error <= 4 * 2^-24 r) also carries
+// = 10 * 2^-24 r for kFarFactor = 1/8 -- about 6e-7 relative at worst, the
+// order of the FP32 arithmetic of the term.  A very far term (gap >= D/4:
+// displacement error <= 6 * 2^-24 r) also carries
 // the MUFU rsqrt error three times, at most 3.7e-7 and on average -1.6e-8
 // relative (measured over every FP32 input in [1, 4), i.e. every mantissa at
 // both exponent parities); these terms are many and distant,
-// so their errors average out: on the same sphere the maximum relative force
-// error stays at 7e-7 and the RMS at 3e-8.  Near terms keep the double-single
+// so their errors average out: on a 65,536-body Plummer sphere the far /
+// very-far factors (1/8, 1/4), (1/4, 1/4), (1/4, 1/2), (1/2, 1/2) and (1/2, 1)
+// give the same errors (largest relative 5e-7 where S_i / |a_i| <= 10, RMS
+// 2.5e-8), and (1/8, 1/4) the shortest kernel (2 % under (1/4, 1/2)).  Near terms keep the double-single
 // displacement (absolute error ~2^-48 |x|) and the Newton step; every FP32
-// accumulator takes 32 terms before its Kahan-compensated add, and the
+// accumulator takes 16 terms before its Kahan-compensated add, and the
 // segments combine as a double-single.
 #include "nb_internal.h"
 #include "nb_pair.cuh"
@@ -54,11 +58,12 @@ namespace nb {
 namespace {
 
 constexpr int kChunk = 32;             // j-chunk = one body per lane
-constexpr float kFarFactor2 = 0.0625f; // (gap / D)^2 threshold: kFarFactor = 1/4
-constexpr float kVeryFar2 = 0.25f;      // (gap / D)^2 threshold without Newton: 1/2
-constexpr int kResortEvals = 8;        // force evaluations per Morton re-sort
+constexpr float kFarFactor2 = 0.015625f; // (gap / D)^2 threshold: kFarFactor = 1/8
+constexpr float kVeryFar2 = 0.0625f;     // (gap / D)^2 threshold without Newton: 1/4
+constexpr int kResortEvals = 8;        // force evaluations per re-sort
+constexpr bool kHilbertOrder = true;   // sort along the Hilbert curve (else Morton)
 
-// Positions in Morton order relative to the root centre, split into
+// Positions in sorted order relative to the root centre, split into
 // double-single hi/lo parts; mass in hi.w.
 __global__ void split_sorted_kernel(const uint32_t *__restrict__ order,
                                     const double *__restrict__ x, const double *__restrict__ y,
@@ -116,6 +121,15 @@ __device__ __forceinline__ void rel_ds(float h, float l, float c, float &S, floa
     float s, e;
     two_sum(h, -c, s, e);
     two_sum(s, e + l, S, E);
+}
+
+// (h + l) - c rounded to FP32: the S of rel_ds (one rounding of the exact
+// difference, up to the ~2^-48 |h| of the low-order add) without the E.
+__device__ __forceinline__ float rel_s(float h, float l, float c)
+{
+    float s, e;
+    two_sum(h, -c, s, e);
+    return s + (e + l);
 }
 
 // One warp = 32*IPT consecutive sorted i-bodies (chunks tile0 .. tile0+IPT-1,
@@ -190,7 +204,6 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
         h = hi[jc0 * kChunk + lane];
         l = lo[jc0 * kChunk + lane];
     }
-    int pending = 0;  // chunks in the FP32 accumulators since the last Kahan add
     for (int jc = jc0; jc < jc1; ++jc) {
         const float4 jmn = box[2 * jc], jmx = box[2 * jc + 1];
         const float gx = fmaxf(0.f, fmaxf(jmn.x - bmx[0], bmn[0] - jmx.x));
@@ -203,13 +216,22 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
         // lanes past n stage a massless body far away: its terms are exactly 0
         float Sx = 1.0e18f, Sy = 1.0e18f, Sz = 1.0e18f, Ex = 0.f, Ey = 0.f, Ez = 0.f, mj = 0.f;
         if (valid) {
-            rel_ds(h.x, l.x, cx, Sx, Ex);
-            rel_ds(h.y, l.y, cy, Sy, Ey);
-            rel_ds(h.z, l.z, cz, Sz, Ez);
+            if (far) {  // S alone: x - c rounded once
+                Sx = rel_s(h.x, l.x, cx);
+                Sy = rel_s(h.y, l.y, cy);
+                Sz = rel_s(h.z, l.z, cz);
+            } else {
+                rel_ds(h.x, l.x, cx, Sx, Ex);
+                rel_ds(h.y, l.y, cy, Sy, Ey);
+                rel_ds(h.z, l.z, cz, Sz, Ez);
+            }
             mj = h.w;
         }
         __syncwarp();
-        pair_tile_put(sg, lane, Sx, Sy, Sz, mj, Ex, Ey, Ez);
+        if (far)
+            pair_tile_put_hi(sg, lane, Sx, Sy, Sz, mj);
+        else
+            pair_tile_put(sg, lane, Sx, Sy, Sz, mj, Ex, Ey, Ez);
         __syncwarp();
         valid = jc + 1 < jc1 && (jc + 1) * kChunk + lane < n;
         if (valid) {
@@ -243,16 +265,15 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
                                           ax[k], ay[k], az[k]);
             }
         }
-        // every accumulator lane holds 16 terms per chunk: fold after two
-        if (++pending == 2 || jc + 1 == jc1) {
+        // every accumulator lane holds 16 terms of the chunk: fold them into the
+        // Kahan sums (folding after every second chunk measured no faster, and
+        // raised the largest relative error at N = 65,536 from 6e-7 to 9e-7)
 #pragma unroll
-            for (int k = 0; k < IPT; ++k) {
-                kahan_add(sx[k], qx[k], ax[k].x + ax[k].y);
-                kahan_add(sy[k], qy[k], ay[k].x + ay[k].y);
-                kahan_add(sz[k], qz[k], az[k].x + az[k].y);
-                ax[k] = ay[k] = az[k] = dup2(0.f);
-            }
-            pending = 0;
+        for (int k = 0; k < IPT; ++k) {
+            kahan_add(sx[k], qx[k], ax[k].x + ax[k].y);
+            kahan_add(sy[k], qy[k], ay[k].x + ay[k].y);
+            kahan_add(sz[k], qz[k], az[k].x + az[k].y);
+            ax[k] = ay[k] = az[k] = dup2(0.f);
         }
     }
 
@@ -462,8 +483,11 @@ nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
     if (n <= 0) return NB_OK;
     if (!b.sorter) b.sorter = bh_create();
     if (b.order_n != n || b.evals_since_sort >= kResortEvals) {
-        // 10 levels of the Morton curve: cells far smaller than a 32-body chunk
-        NB_TRY(bh_morton_order(b.sorter, x, y, z, n, 10, st, &b.order, &b.centre));
+        // 2^30 cells: far smaller than a 32-body chunk
+        if (kHilbertOrder)
+            NB_TRY(bh_hilbert_order(b.sorter, x, y, z, n, st, &b.order, &b.centre));
+        else
+            NB_TRY(bh_morton_order(b.sorter, x, y, z, n, 10, st, &b.order, &b.centre));
         b.order_n = n;
         b.evals_since_sort = 0;
     }

@@ -88,12 +88,12 @@ DirectPlan direct_mixed_plan(int n);
 // j-split count filling whole waves of `slots` resident CTAs.
 int direct_pick_segments(int iblocks, int tiles, int slots);
 
-// Morton-sorted near/far variant of the mixed path (nb_direct_sorted.cu).
+// Hilbert-sorted near/far variant of the mixed path (nb_direct_sorted.cu).
 struct BHTree;
 struct SortedBuffers {
     DevBuf hi, lo, partials, boxes;
     BHTree *sorter = nullptr;
-    // The Morton order is a performance device only (near/far decisions use
+    // The sort order is a performance device only (near/far decisions use
     // the current chunk boxes, any order gives results within tolerance), so
     // it is recomputed every kResortEvals force evaluations and when n
     // changes -- not at every call, and not on a load (the next periodic
@@ -105,19 +105,19 @@ struct SortedBuffers {
     void invalidate_order() { order_n = -1; }
     void release();
 };
-// Bodies are sorted along a Morton curve; every warp re-centres the j-chunks
-// (32 bodies) that lie at least a quarter of its (compact) i-box diameter away on its
-// own box and runs the plain FP32 pair term on them; near chunks keep the
-// double-single one.
+// Bodies are sorted along a Hilbert curve; every warp re-centres the j-chunks
+// (32 bodies) on its own (compact) i-box and runs the plain FP32 pair term on
+// those that lie at least an eighth of the box diameter away; near chunks keep
+// the double-single one.
 nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
                               const double *m, int n, double G, double eps2, double *ax,
                               double *ay, double *az, SortedBuffers &b, cudaStream_t st,
                               const KernelTimer *timer = nullptr);
 // Whether an evaluation of n bodies takes the sorted variant: flags
 // NB_FLAG_MIXED_SORTED / NB_FLAG_MIXED_UNSORTED decide, else n >= kSortedMinBodies
-// (measured crossover on GB300: the sort and the near chunks cost more than the
-// far chunks save below ~28k bodies of a Plummer sphere).
-constexpr int kSortedMinBodies = 28672;
+// (measured on GB300 per evaluation of a Plummer sphere, unsorted vs sorted:
+// 12,288 bodies 0.120 vs 0.136 ms, 16,384 bodies 0.201 vs 0.194 ms).
+constexpr int kSortedMinBodies = 16384;
 bool direct_sorted_enabled(int n, int flags);
 
 // FP64 all-pairs kernel.
@@ -213,6 +213,10 @@ nb_status bh_info(BHTree *t, cudaStream_t st, nb_bh_info *info);
 nb_status bh_morton_order(BHTree *t, const double *x, const double *y, const double *z, int n,
                           int levels, cudaStream_t st, const uint32_t **order,
                           const double **root_centre);
+// The same for the order along the Hilbert curve through the 2^10-cell grid of
+// the root cube (runs of sorted bodies fill compact regions).
+nb_status bh_hilbert_order(BHTree *t, const double *x, const double *y, const double *z, int n,
+                           cudaStream_t st, const uint32_t **order, const double **root_centre);
 nb_status bh_read_order(BHTree *t, cudaStream_t st, uint64_t *codes, uint32_t *order);
 nb_status bh_read_nodes(BHTree *t, cudaStream_t st, int max_nodes, int *depth,
                         uint64_t *prefix, int *first, int *count, int *is_leaf, int *skip,
@@ -234,7 +238,7 @@ struct nb_sim {
     bool forces_valid = false;
 
     nb::DevBuf split_hi, split_lo;   // float4 mirrors for the mixed kernel
-    nb::SortedBuffers sorted;        // Morton-sorted near/far variant of the mixed kernel
+    nb::SortedBuffers sorted;        // Hilbert-sorted near/far variant of the mixed kernel
     nb::DevBuf partials;             // j-split partial sums
     nb::DevBuf old_acc;              // velocity-Verlet a(t)
     nb::DevBuf rk4;                  // RK4 stage states and accelerations

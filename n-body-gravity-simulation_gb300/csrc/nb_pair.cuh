@@ -124,6 +124,18 @@ __device__ __forceinline__ void pair_tile_put(PairTile &pt, int lane, float x, f
     f[0] = zl;
 }
 
+// The same without the low parts (a tile read only by pair_term2_far).
+__device__ __forceinline__ void pair_tile_put_hi(PairTile &pt, int lane, float x, float y, float z,
+                                                 float m)
+{
+    float *s = reinterpret_cast<float *>(&pt.s[lane >> 1]) + (lane & 1);
+    float *t = reinterpret_cast<float *>(&pt.t[lane >> 1]) + (lane & 1);
+    s[0] = x;
+    s[2] = y;
+    t[0] = z;
+    t[2] = m;
+}
+
 // j-pair p of a tile as f32x2 operands.
 struct JPair {
     float2 x, y, z, m, xl, yl, zl;

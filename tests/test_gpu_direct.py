@@ -133,8 +133,8 @@ SORTED = ["plummer20000", "diskbulge16384", "cube10000_eps0", "pairs_far_origin_
 
 @pytest.mark.parametrize("name", SORTED)
 def test_mixed_sorted_near_far(nb, oracle, name):
-    """The Morton-sorted near/far variant of the mixed kernel (the default from
-    28,672 bodies, forced here by NB_FLAG_MIXED_SORTED): far j-chunks use FP32
+    """The Hilbert-sorted near/far variant of the mixed kernel (the default from
+    16,384 bodies, forced here by NB_FLAG_MIXED_SORTED): far j-chunks use FP32
     coordinates relative to the warp's centre (very far ones without the Newton
     step), near chunks the double-single displacement.  Same tolerances."""
     G, eps = 1.0, 1e-3
