@@ -159,6 +159,28 @@ def test_mixed_sorted_near_far(nb, oracle, name):
     check_mixed(oracle, a, ref, st, G, eps)
 
 
+def test_bench_workload_forces_along_the_trajectory(nb, oracle):
+    """The benchmark workload (65,536-body Plummer sphere, eps 1e-3, velocity
+    Verlet dt 5e-4) run on the mixed path: the accelerations it integrates
+    with after 1, 10 and 100 steps meet the mixed tolerances against the FP64
+    direct sum of the oracle on the same positions (the sorted kernel re-sorts
+    every 8 evaluations, so these states use fresh and aged orders)."""
+    G, eps, dt = 1.0, 1e-3, 5e-4
+    st = nb.plummer(65536, seed=0)
+    with nb.Sim(nb.Config(method=nb.DIRECT_MIXED, G=G, softening=eps),
+                capacity=65536) as s:
+        s.load(*st)
+        done = 0
+        for target in (1, 10, 100):
+            s.step(nb.VELOCITY_VERLET, dt, target - done)
+            done = target
+            cur = s.read_state()
+            pos = (cur["x"], cur["y"], cur["z"])
+            ref = oracle.forces_naive(*pos, cur["m"], G, eps)
+            state = pos + (cur["vx"], cur["vy"], cur["vz"], cur["m"])
+            check_mixed(oracle, (cur["ax"], cur["ay"], cur["az"]), ref, state, G, eps)
+
+
 @pytest.mark.parametrize("n", [37, 1000, 3000])
 def test_mixed_sorted_small_and_ragged(nb, oracle, n):
     """The sorted kernel on sizes that are not multiples of its 32-body chunks
