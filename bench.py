@@ -63,6 +63,9 @@ def parse():
     ap.add_argument("--bh-steps", type=int, default=20,
                     help="leapfrog steps of the Barnes-Hut N=2^20 extra (0 skips it)")
     ap.add_argument("--bh-n", type=int, default=1 << 20)
+    ap.add_argument("--bh-variants", default="rebuild,reuse4,quad",
+                    help="Barnes-Hut variants to run: rebuild every step (the configuration), "
+                         "reuse4 (tree reuse every 4 evaluations), quad (quadrupoles)")
     ap.add_argument("--ens-steps", type=int, default=25,
                     help="RK4 steps of the 4096-system ensemble extra (0 skips it)")
     ap.add_argument("--ens-systems", type=int, default=4096)
@@ -414,17 +417,21 @@ def run_bh(a, nb, torch, dev, stream, flush, np):
                                         "p99_rel": float(np.quantile(rel, 0.99))}
         return out
 
+    variants = set(a.bh_variants.split(","))
     out = {"workload": f"disk_bulge_n{n}_theta{BH_THETA}_leapfrog", "n": n,
            "steps": a.bh_steps}
-    out.update(timed(0))
-    out["timing"] = ("CUDA events per leapfrog step, L2 flushed before each; a build reads "
-                     "the node count on the host once per step")
+    if "rebuild" in variants:
+        out.update(timed(0))
+        out["timing"] = ("CUDA events per leapfrog step, L2 flushed before each; a build "
+                         "reads the node count on the host once per step")
     keys = ("ms_per_step", "steps_per_s", "walk_ms", "interactions_per_body",
             "force_error_vs_direct")
-    reuse = timed(nb.bh_reuse_flag(4))
-    out["tree_reuse_4"] = {k: reuse[k] for k in keys}
-    quad = timed(nb.BH_QUADRUPOLE)
-    out["quadrupole"] = {k: quad[k] for k in keys}
+    if "reuse4" in variants:
+        reuse = timed(nb.bh_reuse_flag(4))
+        out["tree_reuse_4"] = {k: reuse[k] for k in keys}
+    if "quad" in variants:
+        quad = timed(nb.BH_QUADRUPOLE)
+        out["quadrupole"] = {k: quad[k] for k in keys}
     return out
 
 

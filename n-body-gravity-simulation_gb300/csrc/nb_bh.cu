@@ -88,29 +88,73 @@ struct BHStats {
 };
 
 // ------------------------------------------------------------ bounding box
+// An FP64 value as a signed 64-bit key with the same order (negative values
+// have their magnitude bits flipped); the min/max reduction then runs on the
+// integer pipes (GB300's FP64 pipe is a small fraction of them).  NaN maps to
+// the neutral key, so it is ignored as fmin/fmax ignore it.
+__device__ __forceinline__ long long order_key(double v, long long nan_key)
+{
+    const long long b = __double_as_longlong(v);
+    if ((b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll) return nan_key;
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ double key_value(long long k)
+{
+    return __longlong_as_double(k >= 0 ? k : (k ^ 0x7fffffffffffffffll));
+}
+
 __global__ void __launch_bounds__(256)
 bbox_partial_kernel(const double *__restrict__ x, const double *__restrict__ y,
                     const double *__restrict__ z, int n, double *__restrict__ part)
 {
-    __shared__ double sh[6][256];
-    double v[6] = {1e308, 1e308, 1e308, -1e308, -1e308, -1e308};
-    for (int i = blockIdx.x * 256 + threadIdx.x; i < n; i += gridDim.x * 256) {
-        const double a = x[i], b = y[i], c = z[i];
-        v[0] = fmin(v[0], a); v[1] = fmin(v[1], b); v[2] = fmin(v[2], c);
-        v[3] = fmax(v[3], a); v[4] = fmax(v[4], b); v[5] = fmax(v[5], c);
+    constexpr long long kMax = 0x7fffffffffffffffll, kMin = -kMax - 1;
+    __shared__ long long sh[6][8];
+    long long v[6] = {kMax, kMax, kMax, kMin, kMin, kMin};
+    const double *ax[3] = {x, y, z};
+    // four grid strides per iteration: twelve loads in flight per thread
+    const int stride = gridDim.x * 256;
+    int i = blockIdx.x * 256 + threadIdx.x;
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        double p[3][4];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) p[c][u] = ax[c][i + u * stride];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                v[c] = min(v[c], order_key(p[c][u], kMax));
+                v[c + 3] = max(v[c + 3], order_key(p[c][u], kMin));
+            }
     }
-    for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = v[k];
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
-            for (int k = 0; k < 3; ++k)
-                sh[k][threadIdx.x] = fmin(sh[k][threadIdx.x], sh[k][threadIdx.x + w]);
-            for (int k = 3; k < 6; ++k)
-                sh[k][threadIdx.x] = fmax(sh[k][threadIdx.x], sh[k][threadIdx.x + w]);
+    for (; i < n; i += stride)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double q = ax[c][i];
+            v[c] = min(v[c], order_key(q, kMax));
+            v[c + 3] = max(v[c + 3], order_key(q, kMin));
         }
-        __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            v[c] = min(v[c], __shfl_xor_sync(0xffffffffu, v[c], o));
+            v[c + 3] = max(v[c + 3], __shfl_xor_sync(0xffffffffu, v[c + 3], o));
+        }
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sh[c][warp] = v[c];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int c = threadIdx.x;
+        long long r = sh[c][0];
+        for (int w = 1; w < 8; ++w) r = c < 3 ? min(r, sh[c][w]) : max(r, sh[c][w]);
+        // a block that saw only NaN (or nothing) reports the neutral value
+        const bool empty = r == (c < 3 ? kMax : kMin);
+        part[blockIdx.x * 6 + c] = empty ? (c < 3 ? 1e308 : -1e308) : key_value(r);
     }
-    if (threadIdx.x < 6) part[blockIdx.x * 6 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
 // One block: reduce the partials, then thread 0 derives the root cube by the
@@ -180,16 +224,19 @@ __device__ __forceinline__ uint64_t spread21(uint64_t v)
 
 // Fast path of one axis: the cell index on the ideal 2^21 grid of the root
 // cube and whether the position is far enough from every grid line that the
-// CPU tree's rounded running centres cannot compare differently.
-__device__ __forceinline__ bool grid_index(double p, double lo, double scale, double margin,
-                                           uint64_t *q)
+// CPU tree's rounded running centres cannot compare differently.  f carries a
+// few roundings of ~2^-31 grid cells; the margin (>= 1e-6 cells) covers them.
+// Five FP64 operations (the FP64 pipe bounds this kernel): f, its floor as an
+// integer, back to FP64, the fraction, and the fraction in FP32 (an error of
+// ~2^-24, far below the margin) for the two comparisons.
+__device__ __forceinline__ bool grid_index(double p, double lo_scaled, double scale,
+                                           float margin, uint64_t *q)
 {
-    const double f = (p - lo) * scale;
-    double fl = floor(f);
-    fl = fmin(fmax(fl, 0.0), 2097151.0);
+    const double f = fma(p, scale, -lo_scaled);
+    const long long fl = min(max(__double2ll_rd(f), 0ll), 2097151ll);
     *q = (uint64_t)fl;
-    const double d = fmin(f - fl, fl + 1.0 - f);
-    return d > margin;
+    const float frac = __double2float_rn(f - (double)fl);  // in [0, 1) unless clamped
+    return frac > margin && frac < 1.0f - margin;
 }
 
 __global__ void __launch_bounds__(256)
@@ -198,34 +245,36 @@ encode_kernel(const double *__restrict__ x, const double *__restrict__ y,
               uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
 {
     __shared__ double off[kMaxLevels];
-    __shared__ double c0[3], lo[3], scale, margin;
+    __shared__ double c0[3], lo_scaled[3], scale;
+    __shared__ float margin;
     __shared__ int levels;
     if (threadIdx.x < kMaxLevels) off[threadIdx.x] = root->off[threadIdx.x];
     if (threadIdx.x == 0) {
         c0[0] = root->cx; c0[1] = root->cy; c0[2] = root->cz;
         levels = root->levels;
         const double size = root->size;
+        scale = 2097152.0 / size;
         double cmax = 0.0;
         for (int k = 0; k < 3; ++k) {
-            lo[k] = c0[k] - size / 2;
+            lo_scaled[k] = (c0[k] - size / 2) * scale;
             cmax = fmax(cmax, fabs(c0[k]));
         }
-        scale = 2097152.0 / size;
         // Running centres accumulate at most 21 roundings of half an ulp of
-        // |centre| <= cmax + size; the fast index adds a few more roundings.
+        // |centre| <= cmax + size; the fast index adds a few more roundings
+        // (of |p| * scale and of lo * scale: 2^-52 (cmax + size) scale each).
         // Positions farther than this from every grid line index exactly.
         const double u_c = ldexp(1.0, ilogb(cmax + size) - 52);
         const double u_s = ldexp(1.0, ilogb(size) - 52);
-        margin = (24.0 * u_c + 4.0 * u_s) * scale + 1e-6;
+        margin = (float)((32.0 * u_c + 4.0 * u_s) * scale + 1e-6);
     }
     __syncthreads();
     const int i = blockIdx.x * 256 + threadIdx.x;
     if (i >= n) return;
     const double px = x[i], py = y[i], pz = z[i];
     uint64_t qx, qy, qz;
-    const bool okx = grid_index(px, lo[0], scale, margin, &qx);
-    const bool oky = grid_index(py, lo[1], scale, margin, &qy);
-    const bool okz = grid_index(pz, lo[2], scale, margin, &qz);
+    const bool okx = grid_index(px, lo_scaled[0], scale, margin, &qx);
+    const bool oky = grid_index(py, lo_scaled[1], scale, margin, &qy);
+    const bool okz = grid_index(pz, lo_scaled[2], scale, margin, &qz);
     if (okx && oky && okz) {
         uint64_t code = (spread21(qx) << 2) | (spread21(qy) << 1) | spread21(qz);
         const int drop = 3 * (kMaxLevels - levels);  // digits below the split limit are 0
@@ -336,20 +385,27 @@ radix_hist_kernel(const uint64_t *__restrict__ keys, int n, int shift, int *__re
 
 // Stable scatter of one 8-bit digit.  Warp w of the block ranks keys
 // [tile + w*256, +256) in rounds of 32 (lane order), so ranks follow the input
-// order; per-warp digit counts are turned into per-warp offsets, and the
-// tile's global offset per digit comes from the scanned histogram.
+// order; per-warp digit counts are turned into per-warp offsets.  The tile is
+// then put in digit order in shared memory and written out by consecutive
+// threads, so each digit's run of the tile goes to consecutive addresses (the
+// tile's global offset per digit comes from the scanned histogram).
 __global__ void __launch_bounds__(256)
 radix_scatter_kernel(const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin,
                      uint64_t *__restrict__ kout, uint32_t *__restrict__ vout, int n, int shift,
                      const int *__restrict__ offsets, int num_tiles)
 {
     __shared__ int wh[kSortWarps][256];
-    __shared__ int toff[256];
+    __shared__ int toff[256];    // global position of the tile's first key of digit d
+    __shared__ int tstart[256];  // position in the tile of its first key of digit d
+    __shared__ int wsum[kSortWarps];
+    __shared__ uint64_t skey[kSortTile];
+    __shared__ uint32_t sval[kSortTile];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int k = threadIdx.x; k < kSortWarps * 256; k += 256) (&wh[0][0])[k] = 0;
     toff[threadIdx.x] = offsets[threadIdx.x * num_tiles + blockIdx.x];
     __syncthreads();
-    const int base = blockIdx.x * kSortTile + warp * 32 * kSortRounds;
+    const int tile0 = blockIdx.x * kSortTile;
+    const int base = tile0 + warp * 32 * kSortRounds;
     uint64_t key[kSortRounds];
     uint32_t val[kSortRounds];
     int rank[kSortRounds], dig[kSortRounds];
@@ -372,6 +428,8 @@ radix_scatter_kernel(const uint64_t *__restrict__ kin, const uint32_t *__restric
     }
     __syncthreads();
     {
+        // per-warp offsets within the digit, and the tile's digit starts
+        // (exclusive scan of the digit totals: warp shuffles, then warp sums)
         const int d = threadIdx.x;
         int run = 0;
         for (int w = 0; w < kSortWarps; ++w) {
@@ -379,16 +437,36 @@ radix_scatter_kernel(const uint64_t *__restrict__ kin, const uint32_t *__restric
             wh[w][d] = run;
             run += c;
         }
+        int inc = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += u;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        int before = 0;
+        for (int w = 0; w < warp; ++w) before += wsum[w];
+        tstart[d] = before + inc - run;
     }
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < kSortRounds; ++r) {
         const int d = dig[r];
         if (d >= 0) {
-            const int pos = toff[d] + wh[warp][d] + rank[r];
-            kout[pos] = key[r];
-            vout[pos] = val[r];
+            const int lpos = tstart[d] + wh[warp][d] + rank[r];
+            skey[lpos] = key[r];
+            sval[lpos] = val[r];
         }
+    }
+    __syncthreads();
+    const int count = min(kSortTile, n - tile0);
+    for (int j = threadIdx.x; j < count; j += 256) {
+        const uint64_t k = skey[j];
+        const int d = (int)((k >> shift) & 0xFF);
+        const int pos = toff[d] + (j - tstart[d]);
+        kout[pos] = k;
+        vout[pos] = sval[j];
     }
 }
 
@@ -439,6 +517,55 @@ template <> struct Add<D4> {
 constexpr int kScanItems = 4;
 constexpr int kScanTile = 256 * kScanItems;
 
+__device__ __forceinline__ int shfl_up(int v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
+__device__ __forceinline__ D4 shfl_up(const D4 &v, int d)
+{
+    return D4{__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d),
+              __shfl_up_sync(0xffffffffu, v.z, d), __shfl_up_sync(0xffffffffu, v.w, d)};
+}
+
+// Inclusive scan of one value per lane over a warp (shuffles).
+template <class T>
+__device__ __forceinline__ T warp_inclusive(T v, int lane)
+{
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const T u = shfl_up(v, off);
+        if (lane >= off) v = Add<T>::op(u, v);
+    }
+    return v;
+}
+
+// Exclusive scan of one value per thread over a block of NW warps: each warp
+// scans its lanes, warp 0 scans the warp totals (the FP64 pipe is narrow, so
+// no thread adds up all of them itself), and *total receives the block's
+// sum.  Every thread of the block must call it; warp_sums holds NW + 1.
+template <class T, int NW>
+__device__ __forceinline__ T block_exclusive(T s, T *warp_sums, T *total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const T inc = warp_inclusive(s, lane);
+    if (lane == 31) warp_sums[warp] = inc;
+    T excl = shfl_up(inc, 1);
+    if (lane == 0) excl = Add<T>::zero();
+    __syncthreads();
+    if (warp == 0) {
+        const T w = lane < NW ? warp_sums[lane] : Add<T>::zero();
+        const T wi = warp_inclusive(w, lane);
+        T we = shfl_up(wi, 1);
+        if (lane == 0) we = Add<T>::zero();
+        __syncwarp();
+        if (lane < NW) warp_sums[lane] = we;
+        if (lane == NW - 1) warp_sums[NW] = wi;
+    }
+    __syncthreads();
+    *total = warp_sums[NW];
+    return Add<T>::op(warp_sums[warp], excl);
+}
+
+// sums[b] = the sum of tile b (kScanTile elements): a tree in shared memory,
+// whose idle warps skip their steps (fewer FP64 adds than a shuffle
+// reduction, in which every lane adds at every step).
 template <class T>
 __global__ void __launch_bounds__(256)
 scan_reduce_kernel(const T *__restrict__ in, int n, T *__restrict__ sums)
@@ -458,25 +585,18 @@ scan_reduce_kernel(const T *__restrict__ in, int n, T *__restrict__ sums)
     if (threadIdx.x == 0) sums[blockIdx.x] = sh[0];
 }
 
-// Exclusive scan of the block sums in place, one block of 1024 threads.
+// Exclusive scan of the tile sums in place, one block of 1024 threads.
 template <class T>
 __global__ void __launch_bounds__(1024) scan_top_kernel(T *__restrict__ a, int len)
 {
-    __shared__ T sh[1024];
+    __shared__ T warp_sums[33];
     const int t = threadIdx.x;
     const int chunk = (len + 1023) / 1024;
     const int b = t * chunk, e = min(len, b + chunk);
     T s = Add<T>::zero();
     for (int k = b; k < e; ++k) s = Add<T>::op(s, a[k]);
-    sh[t] = s;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const T v = t >= off ? sh[t - off] : Add<T>::zero();
-        __syncthreads();
-        sh[t] = Add<T>::op(sh[t], v);
-        __syncthreads();
-    }
-    T run = t > 0 ? sh[t - 1] : Add<T>::zero();
+    T total;
+    T run = block_exclusive<T, 32>(s, warp_sums, &total);
     for (int k = b; k < e; ++k) {
         const T v = a[k];
         a[k] = run;
@@ -490,7 +610,7 @@ __global__ void __launch_bounds__(256)
 scan_apply_kernel(const T *__restrict__ in, int n, const T *__restrict__ block_off,
                   T *__restrict__ out)
 {
-    __shared__ T sh[256];
+    __shared__ T warp_sums[9];
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     T v[kScanItems];
     T s = Add<T>::zero();
@@ -499,16 +619,8 @@ scan_apply_kernel(const T *__restrict__ in, int n, const T *__restrict__ block_o
         v[k] = base + k < n ? in[base + k] : Add<T>::zero();
         s = Add<T>::op(s, v[k]);
     }
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (int off = 1; off < 256; off <<= 1) {
-        const T u = threadIdx.x >= off ? sh[threadIdx.x - off] : Add<T>::zero();
-        __syncthreads();
-        sh[threadIdx.x] = Add<T>::op(sh[threadIdx.x], u);
-        __syncthreads();
-    }
-    T run = Add<T>::op(block_off[blockIdx.x],
-                       threadIdx.x > 0 ? sh[threadIdx.x - 1] : Add<T>::zero());
+    T total;
+    T run = Add<T>::op(block_off[blockIdx.x], block_exclusive<T, 8>(s, warp_sums, &total));
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
         if (base + k < n) out[base + k] = run;
@@ -604,6 +716,25 @@ chain_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__res
     chain_depth[i] = a;
 }
 
+// (centre of mass, mass) of the bodies between two prefix sums of
+// (m, m x, m y, m z): the differences in FP64 (exact enough: the sums are
+// FP64), the division in FP32 (two roundings more than an FP64 division
+// rounded to FP32, ~1e-7 of the position; the FP64 pipe is a small fraction
+// of the FP32 one and three FP64 divisions per node dominated this kernel).
+__device__ __forceinline__ float4 monopole(const D4 &lo, const D4 &hi)
+{
+    const double mass = hi.x - lo.x;
+    if (!(mass > 0.0)) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const float m = (float)mass;
+    if (m > 1e-30f && m < 1e30f) {
+        const float r = 1.0f / m;
+        return make_float4((float)(hi.y - lo.y) * r, (float)(hi.z - lo.z) * r,
+                           (float)(hi.w - lo.w) * r, m);
+    }
+    return make_float4((float)((hi.y - lo.y) / mass), (float)((hi.z - lo.z) / mass),
+                       (float)((hi.w - lo.w) / mass), m);  // outside FP32's comfortable range
+}
+
 __global__ void __launch_bounds__(256)
 node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__restrict__ root,
             const int *__restrict__ chain_len, const int *__restrict__ chain_depth,
@@ -623,14 +754,8 @@ node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__rest
         const int d = a + k;
         const int cnt = cell_end(c, n, i, d) - i;
         const bool leaf = !(cnt > cap && d < levels);
-        const D4 hi = P[i + cnt], lo = P[i];
-        const double mass = hi.x - lo.x;
-        float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (mass > 0.0)
-            cm = make_float4((float)((hi.y - lo.y) / mass), (float)((hi.z - lo.z) / mass),
-                             (float)((hi.w - lo.w) / mass), (float)mass);
         BHNode nd;
-        nd.com_mass = cm;
+        nd.com_mass = monopole(P[i], P[i + cnt]);
         nd.first = i;
         nd.count = cnt;
         nd.skip = offsets[i + cnt];
@@ -666,12 +791,7 @@ refit_kernel(BHNode *__restrict__ nodes, const int *__restrict__ total,
     const int k = blockIdx.x * 256 + threadIdx.x;
     if (k >= *total) return;
     BHNode nd = nodes[k];
-    const D4 hi = P[nd.first + nd.count], lo = P[nd.first];
-    const double mass = hi.x - lo.x;
-    nd.com_mass = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (mass > 0.0)
-        nd.com_mass = make_float4((float)((hi.y - lo.y) / mass), (float)((hi.z - lo.z) / mass),
-                                  (float)((hi.w - lo.w) / mass), (float)mass);
+    nd.com_mass = monopole(P[nd.first], P[nd.first + nd.count]);
     if (nd.skip == k + 1) {  // leaf
         float4 mn = body[nd.first], mx = mn;
         for (int b = nd.first + 1; b < nd.first + nd.count; ++b) {
@@ -1086,7 +1206,7 @@ static nb_status morton_sort(BHTree *t, const double *x, const double *y, const 
                              int n, int first_shift, cudaStream_t st, bool hilbert = false)
 {
     const size_t N = (size_t)n;
-    const int nparts = std::min(div_up(n, 256), 2 * device_props().num_sms);
+    const int nparts = std::min(div_up(n, 1024), 4 * device_props().num_sms);
     const int num_tiles = div_up(n, kSortTile);
     NB_TRY(t->part.reserve(sizeof(double) * 6 * nparts));
     NB_TRY(t->root.reserve(sizeof(BHRoot)));
