@@ -42,7 +42,8 @@ typedef enum nb_status {
     NB_ERR_NOT_LOADED = 5,   /* no bodies loaded yet */
     NB_ERR_DEVICE_FAULT = 6, /* a kernel reported an error status */
     NB_ERR_UNSUPPORTED = 7,
-    NB_ERR_IO = 8            /* a file could not be opened, read, parsed or written */
+    NB_ERR_IO = 8,           /* a file could not be opened, read, parsed or written */
+    NB_ERR_CANCELLED = 9     /* a serving job was cancelled before it finished */
 } nb_status;
 
 /* Force methods.
@@ -313,6 +314,10 @@ typedef struct nb_server_stats {
     /* parts of host_issue_ms: rebuilding the direct work queue, issuing the
      * direct batch, waiting for the Barnes-Hut stream threads */
     double host_upload_ms, host_direct_ms, host_join_ms;
+    /* jobs that ended without a result: a failure of their own (an allocation
+     * or launch error while admitting or stepping them; the other jobs carry
+     * on) or nb_server_cancel */
+    uint64_t jobs_failed, jobs_cancelled;
 } nb_server_stats;
 
 /* G 1, softening 1e-3, theta 0.6, leaf 8, direct below 16384 bodies, dt 1e-3,
@@ -324,13 +329,24 @@ nb_status nb_server_destroy(nb_server *s);
 nb_status nb_server_submit(nb_server *s, size_t n, const double *x, const double *y,
                            const double *z, const double *vx, const double *vy,
                            const double *vz, const double *m, int steps, int64_t *job_id);
+/* Admits what fits, advances every running job one step, retires finished
+ * jobs.  A failure that belongs to one Barnes-Hut job (its allocation, load or
+ * step returned an error) ends that job alone -- its result then reports the
+ * error -- and the tick still returns NB_OK; a failure of the shared direct
+ * batch or of the device fails the tick. */
 nb_status nb_server_tick(nb_server *s, int *running, int *queued);
-/* State of a finished job (NB_ERR_NOT_LOADED until it finished). */
+/* State of a finished job (NB_ERR_NOT_LOADED until it finished; a job that
+ * failed returns the status it failed with, its message in nb_last_error();
+ * a cancelled one NB_ERR_CANCELLED). */
 nb_status nb_server_result(nb_server *s, int64_t job_id, double *x, double *y, double *z,
                            double *vx, double *vy, double *vz, double *ax, double *ay,
                            double *az, double *m);
 /* Drops a finished job's stored result. */
 nb_status nb_server_release(nb_server *s, int64_t job_id);
+/* Cancels a queued or running job between ticks: its device memory and pool
+ * slot are freed at once and its result becomes NB_ERR_CANCELLED.  A job that
+ * already finished, or an unknown id, is NB_ERR_INVALID_ARGUMENT. */
+nb_status nb_server_cancel(nb_server *s, int64_t job_id);
 nb_status nb_server_get_stats(nb_server *s, nb_server_stats *out);
 
 /* ---- host-side input generators (no GPU needed) ------------------------- */
@@ -445,6 +461,13 @@ const char *nb_last_error(void);
 
 /* Library version string. */
 const char *nb_version(void);
+
+/* Test hook for failure handling (host side only: no CUDA call fails and the
+ * device is untouched).  After `after` more successful device allocations by
+ * this library, in any object of the process, the next one fails with
+ * NB_ERR_OUT_OF_MEMORY and the message "injected allocation failure"; the hook
+ * then disarms.  A negative value disarms it. */
+nb_status nb_debug_fail_device_allocations(int after);
 
 #ifdef __cplusplus
 }

@@ -58,6 +58,8 @@ struct Job {
     Clock::time_point submitted, admitted;
     bool finished = false;
     cudaEvent_t step_done = nullptr;
+    nb_status status = NB_OK;   // a failure of this job alone, or NB_ERR_CANCELLED
+    std::string error;
 };
 
 // First-fit free list over [0, capacity) body slots.
@@ -142,7 +144,7 @@ struct nb_server {
     // statistics
     std::vector<double> step_ms, queue_ms;
     double interactions = 0.0, busy_ms = 0.0;
-    uint64_t submitted = 0, steps_done = 0, ticks = 0;
+    uint64_t submitted = 0, steps_done = 0, ticks = 0, failed = 0, cancelled = 0;
     int max_running = 0;
     double admit_ms = 0.0, issue_ms = 0.0, wait_ms = 0.0, retire_ms = 0.0;
     double upload_ms = 0.0, direct_ms = 0.0, join_ms = 0.0;  // parts of issue_ms
@@ -170,6 +172,34 @@ nb_status upload_systems(nb_server *s, const std::vector<Job *> &jobs, DevBuf &d
                                 cudaMemcpyHostToDevice, s->stream));
     NB_CUDA_TRY(cudaStreamSynchronize(s->stream));
     return NB_OK;
+}
+
+// Frees a running job's device state (pool slot, or its simulation and its
+// share of the budget) and its event.  Only between ticks: nothing of the job
+// is in flight then.
+void drop_resources(nb_server *s, Job *j)
+{
+    if (j->direct) {
+        s->slots.give(j->first, j->n);
+    } else if (j->sim) {
+        nb_destroy(j->sim);
+        j->sim = nullptr;
+        s->bh_bytes -= kBHBytesPerBody * j->n;
+    }
+    if (j->step_done) cudaEventDestroy(j->step_done);
+    j->step_done = nullptr;
+    s->items_dirty = true;
+}
+
+// Moves a job that ends without a result (failed or cancelled) to the
+// finished table.
+void end_job(nb_server *s, std::unique_ptr<Job> j)
+{
+    j->finished = true;
+    if (j->status == NB_ERR_CANCELLED) ++s->cancelled;
+    else ++s->failed;
+    const int64_t id = j->id;
+    s->finished[id] = std::move(j);
 }
 
 nb_status admit(nb_server *s, std::vector<Job *> &new_direct)
@@ -200,12 +230,27 @@ nb_status admit(nb_server *s, std::vector<Job *> &new_direct)
                 c.theta = s->cfg.theta;
                 c.leaf_capacity = s->cfg.leaf_capacity;
                 j->stream_index = (int)(j->id % kBHStreams);
-                NB_TRY(nb_create(&c, j->n, s->bh_streams[j->stream_index], &j->sim));
+                cudaStream_t st = s->bh_streams[j->stream_index];
                 const double *p = j->init.data();
                 const size_t n = j->n;
-                NB_TRY(nb_load(j->sim, n, p, p + n, p + 2 * n, p + 3 * n, p + 4 * n, p + 5 * n,
-                               p + 6 * n));
-                NB_CUDA_TRY(cudaStreamSynchronize(s->bh_streams[j->stream_index]));
+                nb_status r = nb_create(&c, n, st, &j->sim);
+                if (r == NB_OK)
+                    r = nb_load(j->sim, n, p, p + n, p + 2 * n, p + 3 * n, p + 4 * n,
+                                p + 5 * n, p + 6 * n);
+                if (r == NB_OK) {
+                    const cudaError_t e = cudaStreamSynchronize(st);
+                    if (e != cudaSuccess) r = cuda_fail(e, "cudaStreamSynchronize");
+                }
+                if (r != NB_OK) {  // this job alone fails; the others carry on
+                    j->status = r;
+                    j->error = nb_last_error();
+                    if (j->sim) nb_destroy(j->sim);
+                    j->sim = nullptr;
+                    std::vector<double>().swap(j->init);
+                    end_job(s, std::move(*it));
+                    it = s->queue.erase(it);
+                    continue;
+                }
                 s->bh_bytes += need;
                 ok = true;
             }
@@ -231,6 +276,12 @@ nb_status retire(nb_server *s)
 {
     for (auto it = s->running.begin(); it != s->running.end();) {
         Job *j = it->get();
+        if (j->status != NB_OK) {  // failed while stepping: free it, keep the error
+            drop_resources(s, j);
+            end_job(s, std::move(*it));
+            it = s->running.erase(it);
+            continue;
+        }
         if (j->done < j->steps) {
             ++it;
             continue;
@@ -309,12 +360,13 @@ nb_status tick(nb_server *s)
         }
         for (Job *j : per_stream[k]) {
             nb_status r = nb_step(j->sim, NB_LEAPFROG, dt, 1);
-            if (r == NB_OK && cudaEventRecord(j->step_done, s->bh_streams[k]) != cudaSuccess)
-                r = cuda_fail(cudaGetLastError(), "cudaEventRecord");
-            if (r != NB_OK) {
-                bh_status[k] = r;
-                bh_error[k] = nb_last_error();
-                return;
+            if (r == NB_OK) {
+                const cudaError_t e = cudaEventRecord(j->step_done, s->bh_streams[k]);
+                if (e != cudaSuccess) r = cuda_fail(e, "cudaEventRecord");
+            }
+            if (r != NB_OK) {  // this job alone fails; it is retired below
+                j->status = r;
+                j->error = nb_last_error();
             }
         }
     };
@@ -373,6 +425,7 @@ nb_status tick(nb_server *s)
         }
     }
     for (Job *j : bh) {
+        if (j->status != NB_OK) continue;
         float ms = 0.f;
         NB_CUDA_TRY(cudaEventElapsedTime(&ms, s->tick_start, j->step_done));
         tick_ms = std::max(tick_ms, ms);
@@ -380,7 +433,8 @@ nb_status tick(nb_server *s)
         ++j->done;  // its interactions are read once, at retirement
     }
     s->busy_ms += tick_ms;
-    s->steps_done += direct.size() + bh.size();
+    s->steps_done += direct.size();
+    for (Job *j : bh) s->steps_done += j->status == NB_OK;
     ++s->ticks;
     t_phase = Clock::now();
     const nb_status r = retire(s);
@@ -511,6 +565,7 @@ nb_status nb_server_result(nb_server *s, int64_t job_id, double *x, double *y, d
     auto it = s->finished.find(job_id);
     if (it == s->finished.end()) return fail(NB_ERR_NOT_LOADED, "job not finished (or unknown)");
     const Job *j = it->second.get();
+    if (j->status != NB_OK) return fail(j->status, "job " + std::to_string(job_id) + ": " + j->error);
     double *dst[10] = {x, y, z, vx, vy, vz, ax, ay, az, m};
     for (int k = 0; k < 10; ++k)
         if (dst[k]) std::memcpy(dst[k], j->result.data() + k * j->n, j->n * sizeof(double));
@@ -522,6 +577,34 @@ nb_status nb_server_release(nb_server *s, int64_t job_id)
     if (!s) return fail(NB_ERR_INVALID_ARGUMENT, "server is NULL");
     s->finished.erase(job_id);
     return NB_OK;
+}
+
+nb_status nb_server_cancel(nb_server *s, int64_t job_id)
+{
+    if (!s) return fail(NB_ERR_INVALID_ARGUMENT, "server is NULL");
+    for (auto it = s->queue.begin(); it != s->queue.end(); ++it)
+        if ((*it)->id == job_id) {
+            (*it)->status = NB_ERR_CANCELLED;
+            (*it)->error = "cancelled while queued";
+            std::vector<double>().swap((*it)->init);
+            end_job(s, std::move(*it));
+            s->queue.erase(it);
+            return NB_OK;
+        }
+    for (auto it = s->running.begin(); it != s->running.end(); ++it)
+        if ((*it)->id == job_id) {
+            // between ticks every stream of the server is idle (a tick ends
+            // with them synchronised), so the job's memory can go at once
+            (*it)->status = NB_ERR_CANCELLED;
+            (*it)->error = "cancelled after " + std::to_string((*it)->done) + " steps";
+            drop_resources(s, it->get());
+            end_job(s, std::move(*it));
+            s->running.erase(it);
+            return NB_OK;
+        }
+    return fail(NB_ERR_INVALID_ARGUMENT, s->finished.count(job_id)
+                                             ? "job " + std::to_string(job_id) + " already finished"
+                                             : "unknown job " + std::to_string(job_id));
 }
 
 nb_status nb_server_get_stats(nb_server *s, nb_server_stats *out)
@@ -548,6 +631,8 @@ nb_status nb_server_get_stats(nb_server *s, nb_server_stats *out)
     out->host_upload_ms = s->upload_ms;
     out->host_direct_ms = s->direct_ms;
     out->host_join_ms = s->join_ms;
+    out->jobs_failed = s->failed;
+    out->jobs_cancelled = s->cancelled;
     return NB_OK;
 }
 

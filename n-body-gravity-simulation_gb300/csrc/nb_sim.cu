@@ -22,6 +22,7 @@ namespace nb {
 namespace {
 thread_local std::string g_last_error;
 std::atomic<uint64_t> g_launches{0};
+std::atomic<int> g_fail_allocs_after{-1};  // nb_debug_fail_device_allocations
 constexpr size_t kMaxTimers = 1 << 14;
 
 // The next free event pair of a profiling simulation, or nullptr.
@@ -64,6 +65,11 @@ nb_status DevBuf::reserve(size_t want)
 {
     if (want <= bytes && ptr) return NB_OK;
     release();
+    // the test hook: count down armed allocations, fail the one at zero
+    int armed = g_fail_allocs_after.load();
+    while (armed >= 0 && !g_fail_allocs_after.compare_exchange_weak(armed, armed - 1)) {
+    }
+    if (armed == 0) return fail(NB_ERR_OUT_OF_MEMORY, "injected allocation failure");
     cudaError_t e = cudaMalloc(&ptr, want);
     if (e != cudaSuccess) {
         ptr = nullptr;
@@ -599,6 +605,7 @@ const char *nb_status_string(nb_status s)
     case NB_ERR_DEVICE_FAULT: return "device-reported error";
     case NB_ERR_UNSUPPORTED: return "unsupported";
     case NB_ERR_IO: return "file input/output error";
+    case NB_ERR_CANCELLED: return "cancelled";
     }
     return "unknown status";
 }
@@ -606,5 +613,11 @@ const char *nb_status_string(nb_status s)
 const char *nb_last_error(void) { return g_last_error.c_str(); }
 
 const char *nb_version(void) { return "nbody-gb300 0.1 (sm_103a)"; }
+
+nb_status nb_debug_fail_device_allocations(int after)
+{
+    g_fail_allocs_after.store(after < 0 ? -1 : after);
+    return NB_OK;
+}
 
 } // extern "C"

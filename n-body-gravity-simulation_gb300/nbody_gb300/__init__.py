@@ -31,7 +31,7 @@ EULER, EULER_CROMER, LEAPFROG, VELOCITY_VERLET, RK4 = 0, 1, 2, 3, 4
 
 STATUS = {0: "NB_OK", 1: "NB_ERR_INVALID_ARGUMENT", 2: "NB_ERR_CUDA", 3: "NB_ERR_OUT_OF_MEMORY",
           4: "NB_ERR_CAPACITY", 5: "NB_ERR_NOT_LOADED", 6: "NB_ERR_DEVICE_FAULT",
-          7: "NB_ERR_UNSUPPORTED", 8: "NB_ERR_IO"}
+          7: "NB_ERR_UNSUPPORTED", 8: "NB_ERR_IO", 9: "NB_ERR_CANCELLED"}
 
 # Every function declared in include/nbody_c.h (checked by the tests).
 EXPORTS = [
@@ -50,6 +50,7 @@ EXPORTS = [
     "nb_ensemble_synchronize", "nb_ensemble_info", "nb_ensemble_profile",
     "nb_server_config_default", "nb_server_create", "nb_server_destroy", "nb_server_submit",
     "nb_server_tick", "nb_server_result", "nb_server_release", "nb_server_get_stats",
+    "nb_server_cancel", "nb_debug_fail_device_allocations",
 ]
 _NON_STATUS = {"nb_status_string", "nb_last_error", "nb_version", "nb_kernel_launch_count"}
 
@@ -110,7 +111,8 @@ class _ServerStats(C.Structure):
                 ("host_admit_ms", C.c_double), ("host_issue_ms", C.c_double),
                 ("host_wait_ms", C.c_double), ("host_retire_ms", C.c_double),
                 ("host_upload_ms", C.c_double), ("host_direct_ms", C.c_double),
-                ("host_join_ms", C.c_double)]
+                ("host_join_ms", C.c_double),
+                ("jobs_failed", C.c_uint64), ("jobs_cancelled", C.c_uint64)]
 
 
 def kernel_launch_count() -> int:
@@ -215,6 +217,8 @@ def lib():
     L.nb_server_result.argtypes = [vp, C.c_int64] + [vp] * 10
     L.nb_server_release.argtypes = [vp, C.c_int64]
     L.nb_server_get_stats.argtypes = [vp, C.POINTER(_ServerStats)]
+    L.nb_server_cancel.argtypes = [vp, C.c_int64]
+    L.nb_debug_fail_device_allocations.argtypes = [C.c_int]
     for name in EXPORTS:
         f = getattr(L, name)
         if name not in _NON_STATUS:
@@ -579,6 +583,10 @@ class Server:
     def release(self, job_id: int):
         _check(lib().nb_server_release(self._h, job_id), "nb_server_release")
 
+    def cancel(self, job_id: int):
+        """Cancels a queued or running job (nb_server_cancel)."""
+        _check(lib().nb_server_cancel(self._h, job_id), "nb_server_cancel")
+
     def stats(self) -> dict:
         s = _ServerStats()
         _check(lib().nb_server_get_stats(self._h, C.byref(s)), "nb_server_get_stats")
@@ -622,3 +630,11 @@ def _bh_info_dict(info) -> dict:
 
 def version() -> str:
     return lib().nb_version().decode()
+
+
+def debug_fail_device_allocations(after: int):
+    """Test hook (nb_debug_fail_device_allocations): the device allocation
+    after `after` more successful ones fails with NB_ERR_OUT_OF_MEMORY;
+    negative disarms.  Host side only."""
+    _check(lib().nb_debug_fail_device_allocations(int(after)),
+           "nb_debug_fail_device_allocations")
