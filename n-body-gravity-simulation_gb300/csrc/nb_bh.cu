@@ -1311,6 +1311,7 @@ void walk_launch(BHTree *t, int n, float theta2, float eps2, double G, double *a
 static nb_status launch_walk(BHTree *t, int n, double G, double eps2, double theta, double *ax,
                              double *ay, double *az, cudaStream_t st, const KernelTimer *timer)
 {
+    NvtxRange range("bh_walk");
     const float th2 = (float)(theta * theta), e2 = (float)eps2;
     if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
     if (t->with_quad) {
@@ -1393,6 +1394,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
         return launch_walk(t, n, G, eps2, theta, ax, ay, az, st, timer);
     }
     t->tree_valid = false;
+    NvtxRange range("bh_build");
     const size_t N = (size_t)n;
     NB_TRY(t->body.reserve(sizeof(float4) * N));
     NB_TRY(t->moments.reserve(sizeof(D4) * N));

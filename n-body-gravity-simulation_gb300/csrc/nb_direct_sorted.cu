@@ -481,6 +481,7 @@ nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
                               SortedBuffers &b, cudaStream_t st, const KernelTimer *timer)
 {
     if (n <= 0) return NB_OK;
+    NvtxRange range("direct_sorted");
     if (!b.sorter) b.sorter = bh_create();
     if (b.order_n != n || b.evals_since_sort >= kResortEvals) {
         // 2^30 cells: far smaller than a 32-body chunk

@@ -299,6 +299,7 @@ nb_status nb_ensemble_compute_forces(nb_ensemble *e)
 
 nb_status nb_ensemble_step(nb_ensemble *e, int integrator, double dt, int nsteps)
 {
+    NvtxRange range("nb_ensemble_step");
     if (!e) return fail(NB_ERR_INVALID_ARGUMENT, "ensemble is NULL");
     if (integrator < NB_EULER || integrator > NB_RK4)
         return fail(NB_ERR_INVALID_ARGUMENT, "unknown integrator");

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstddef>
 #include <cstdint>
@@ -45,6 +46,17 @@ enum DeviceError : int {
     kDevStackOverflow = 1,   // Barnes-Hut walk stack full
     kDevTreeOverflow = 2,    // more nodes than the node buffer holds
     kDevBadInput = 3,        // non-finite coordinates
+};
+
+// An NVTX range over a host scope: the phases of a step (sort, build, walk,
+// direct sum, serving tick) appear by name in timeline profilers and can be
+// selected with ncu --nvtx --nvtx-include; a few nanoseconds when no tool is
+// attached.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
 };
 
 // ---------------------------------------------------------------- memory

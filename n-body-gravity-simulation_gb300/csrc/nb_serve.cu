@@ -322,6 +322,7 @@ double ms_since(Clock::time_point t0)
 
 nb_status tick(nb_server *s)
 {
+    NvtxRange range("server_tick");
     std::vector<Job *> new_direct;
     auto t_phase = Clock::now();
     NB_TRY(admit(s, new_direct));

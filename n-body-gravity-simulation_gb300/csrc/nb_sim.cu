@@ -489,6 +489,7 @@ nb_status nb_num_bodies(const nb_sim *s, size_t *n)
 
 nb_status nb_compute_forces(nb_sim *s)
 {
+    NvtxRange range("nb_compute_forces");
     if (!s) return fail(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
     if (s->n == 0) return fail(NB_ERR_NOT_LOADED, "no bodies loaded");
     NB_TRY(eval_forces(s, s->x(), s->y(), s->z(), s->ax(), s->ay(), s->az()));
@@ -498,6 +499,7 @@ nb_status nb_compute_forces(nb_sim *s)
 
 nb_status nb_step(nb_sim *s, int integrator, double dt, int nsteps)
 {
+    NvtxRange range("nb_step");
     if (!s) return fail(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
     if (nsteps < 0) return fail(NB_ERR_INVALID_ARGUMENT, "nsteps must be >= 0");
     if (integrator < NB_EULER || integrator > NB_RK4)
