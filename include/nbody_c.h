@@ -19,9 +19,11 @@
  *     the reference uses).  Functions that return host data synchronise that
  *     stream; the others are asynchronous.  nb_synchronize() waits.
  *   - A simulation object is not thread-safe; distinct objects are.
- *   - No function prints or exits; a device-side failure (tree or stack
- *     capacity) is reported as NB_ERR_DEVICE_FAULT at the next synchronising
- *     call.
+ *   - No function prints or exits.  Kernels have no failure modes of their
+ *     own: the Barnes-Hut walk is stackless and its node storage is sized to
+ *     an upper bound of the node count before the build, so the reference's
+ *     stack and node-pool overflows cannot occur; NB_ERR_DEVICE_FAULT is
+ *     reserved for device-side checks.
  */
 #ifndef NBODY_C_H
 #define NBODY_C_H

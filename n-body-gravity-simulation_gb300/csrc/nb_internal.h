@@ -40,14 +40,6 @@ void count_launch();
         if (nb_s_ != NB_OK) return nb_s_;                                  \
     } while (0)
 
-// Device status word codes written by kernels (never trap, never hang).
-enum DeviceError : int {
-    kDevOk = 0,
-    kDevStackOverflow = 1,   // Barnes-Hut walk stack full
-    kDevTreeOverflow = 2,    // more nodes than the node buffer holds
-    kDevBadInput = 3,        // non-finite coordinates
-};
-
 // An NVTX range over a host scope: the phases of a step (sort, build, walk,
 // direct sum, serving tick) appear by name in timeline profilers and can be
 // selected with ncu --nvtx --nvtx-include; a few nanoseconds when no tool is
