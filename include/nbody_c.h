@@ -239,10 +239,15 @@ nb_status nb_bh_read_nodes(nb_sim *sim, int max_nodes, int *depth, uint64_t *pre
  * independent systems of uneven N, concatenated in system order, advanced
  * together: mixed-precision direct forces of all systems in one persistent
  * launch over a per-system work queue, per-body updates over the
- * concatenation, the step loop captured in a CUDA graph and replayed.
- * i-bodies per lane are autotuned per N bucket on the loaded systems at the
- * first evaluation (or by nb_ensemble_tune).  A system's result does not
- * depend on the other systems of the ensemble. */
+ * concatenation, the step loop captured in a CUDA graph and replayed.  By
+ * default every system is sorted along a Hilbert curve through its own cube
+ * (at the start of each nb_ensemble_step call, every 25 steps within it, and
+ * in nb_ensemble_compute_forces) and far 32-body chunks take the plain FP32
+ * pair term, as in the single-system sorted kernel; cfg->flags
+ * NB_FLAG_MIXED_UNSORTED selects the all-pairs kernel, whose i-bodies per lane
+ * are autotuned per N bucket on the loaded systems at the first evaluation (or
+ * by nb_ensemble_tune).  Either way a system's result does not depend on the
+ * other systems of the ensemble. */
 typedef struct nb_ensemble nb_ensemble;
 
 typedef struct nb_ensemble_info_t {

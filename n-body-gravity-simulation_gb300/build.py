@@ -59,6 +59,7 @@ def _compile(src: str, obj: str, headers, extra, verbose: bool, force: bool):
 def build(force: bool = False, verbose_ptxas: bool = False, jobs: int | None = None) -> str:
     os.makedirs(BUILD, exist_ok=True)
     headers = sorted(glob.glob(os.path.join(CSRC, "*.h")) +
+                     glob.glob(os.path.join(CSRC, "*.cuh")) +
                      glob.glob(os.path.join(REPO, "include", "*.h")))
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")) +
                      glob.glob(os.path.join(CSRC, "*.cpp")))

@@ -40,6 +40,7 @@
 // num_nodes steps: there is no stack to overflow.  Accelerations are scattered
 // back to the original order in FP64, multiplied by G.
 #include "nb_internal.h"
+#include "nb_curve.cuh"
 #include "nb_pair.cuh"
 
 #include <algorithm>
@@ -88,21 +89,6 @@ struct BHStats {
 };
 
 // ------------------------------------------------------------ bounding box
-// An FP64 value as a signed 64-bit key with the same order (negative values
-// have their magnitude bits flipped); the min/max reduction then runs on the
-// integer pipes (GB300's FP64 pipe is a small fraction of them).  NaN maps to
-// the neutral key, so it is ignored as fmin/fmax ignore it.
-__device__ __forceinline__ long long order_key(double v, long long nan_key)
-{
-    const long long b = __double_as_longlong(v);
-    if ((b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll) return nan_key;
-    return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
-}
-__device__ __forceinline__ double key_value(long long k)
-{
-    return __longlong_as_double(k >= 0 ? k : (k ^ 0x7fffffffffffffffll));
-}
-
 __global__ void __launch_bounds__(256)
 bbox_partial_kernel(const double *__restrict__ x, const double *__restrict__ y,
                     const double *__restrict__ z, int n, double *__restrict__ part)
@@ -210,18 +196,6 @@ bbox_final_kernel(const double *__restrict__ part, int nparts, BHRoot *root)
 }
 
 // ------------------------------------------------------------ Morton encode
-// 21 bits -> every third bit of 63 (standard magic-number spreading).
-__device__ __forceinline__ uint64_t spread21(uint64_t v)
-{
-    v &= 0x1fffffull;
-    v = (v | v << 32) & 0x1f00000000ffffull;
-    v = (v | v << 16) & 0x1f0000ff0000ffull;
-    v = (v | v << 8) & 0x100f00f00f00f00full;
-    v = (v | v << 4) & 0x10c30c30c30c30c3ull;
-    v = (v | v << 2) & 0x1249249249249249ull;
-    return v;
-}
-
 // Fast path of one axis: the cell index on the ideal 2^21 grid of the root
 // cube and whether the position is far enough from every grid line that the
 // CPU tree's rounded running centres cannot compare differently.  f carries a
@@ -304,40 +278,6 @@ encode_kernel(const double *__restrict__ x, const double *__restrict__ y,
 }
 
 // ------------------------------------------------------------ Hilbert encode
-// Position on the Hilbert curve through the 2^10 x 2^10 x 2^10 grid of the root
-// cube, following J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc.
-// 707 (2004): the grid coordinates are turned into the curve's "transposed"
-// index by reflections and exchanges from the top bit down, Gray-decoded, and
-// their bits interleaved (axis 0 most significant).  Consecutive indices are
-// face-adjacent cells, so a run of sorted bodies fills a compact region (the
-// Morton curve jumps between distant cells at every level boundary).
-__device__ __forceinline__ uint32_t hilbert_index30(uint32_t a0, uint32_t a1, uint32_t a2)
-{
-    uint32_t X[3] = {a0, a1, a2};
-    for (uint32_t q = 1u << 9; q > 1; q >>= 1) {
-        const uint32_t p = q - 1;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            if (X[i] & q) {
-                X[0] ^= p;  // reflect the low bits of axis 0
-            } else {        // exchange the low bits of axes 0 and i
-                const uint32_t t = (X[0] ^ X[i]) & p;
-                X[0] ^= t;
-                X[i] ^= t;
-            }
-        }
-    }
-    X[1] ^= X[0];
-    X[2] ^= X[1];
-    uint32_t t = 0;
-    for (uint32_t q = 1u << 9; q > 1; q >>= 1)
-        if (X[2] & q) t ^= q - 1;
-    X[0] ^= t;
-    X[1] ^= t;
-    X[2] ^= t;
-    return (uint32_t)((spread21(X[0]) << 2) | (spread21(X[1]) << 1) | spread21(X[2]));
-}
-
 // keys[i] = the 30-bit Hilbert index of body i in bits 33..62 (the bits a
 // 10-level Morton sort orders by), vals[i] = i.
 __global__ void __launch_bounds__(256)
@@ -1202,35 +1142,25 @@ static size_t node_bound(int n, int leaf_capacity)
 // Root cube, 63-bit codes and the stable LSD sort of the code bits
 // [first_shift, 64) (first_shift 0: the full code).  Leaves the sorted codes
 // and the permutation (sorted index -> original index) in t.
-static nb_status morton_sort(BHTree *t, const double *x, const double *y, const double *z,
-                             int n, int first_shift, cudaStream_t st, bool hilbert = false)
+// Key/value ping-pong buffers and digit histograms for n entries.
+static nb_status reserve_sort(BHTree *t, int n)
 {
     const size_t N = (size_t)n;
-    const int nparts = std::min(div_up(n, 1024), 4 * device_props().num_sms);
     const int num_tiles = div_up(n, kSortTile);
-    NB_TRY(t->part.reserve(sizeof(double) * 6 * nparts));
-    NB_TRY(t->root.reserve(sizeof(BHRoot)));
     NB_TRY(t->keys0.reserve(sizeof(uint64_t) * N));
     NB_TRY(t->keys1.reserve(sizeof(uint64_t) * N));
     NB_TRY(t->vals0.reserve(sizeof(uint32_t) * N));
     NB_TRY(t->vals1.reserve(sizeof(uint32_t) * N));
     // digit counts per tile, then their exclusive scan (256 * tiles + 1 each)
     NB_TRY(t->hist.reserve(sizeof(int) * 2 * (256 * (size_t)num_tiles + 1)));
-    BHRoot *root = t->root.as<BHRoot>();
+    return NB_OK;
+}
 
-    bbox_partial_kernel<<<nparts, 256, 0, st>>>(x, y, z, n, t->part.as<double>());
-    NB_LAUNCH_CHECK();
-    bbox_final_kernel<<<1, 256, 0, st>>>(t->part.as<double>(), nparts, root);
-    NB_LAUNCH_CHECK();
-    if (hilbert)
-        hilbert_kernel<<<div_up(n, 256), 256, 0, st>>>(x, y, z, n, root, t->keys0.as<uint64_t>(),
-                                                        t->vals0.as<uint32_t>());
-    else
-        encode_kernel<<<div_up(n, 256), 256, 0, st>>>(x, y, z, n, root,
-                                                       t->keys0.as<uint64_t>(),
-                                                       t->vals0.as<uint32_t>());
-    NB_LAUNCH_CHECK();
-
+// Stable LSD radix sort of (keys0, vals0) by the key bits [first_shift, 64),
+// 8 bits per pass; leaves the sorted keys and values in t.
+static nb_status radix_passes(BHTree *t, int n, int first_shift, cudaStream_t st)
+{
+    const int num_tiles = div_up(n, kSortTile);
     uint64_t *kin = t->keys0.as<uint64_t>(), *kout = t->keys1.as<uint64_t>();
     uint32_t *vin = t->vals0.as<uint32_t>(), *vout = t->vals1.as<uint32_t>();
     int *counts = t->hist.as<int>();
@@ -1247,6 +1177,50 @@ static nb_status morton_sort(BHTree *t, const double *x, const double *y, const 
     }
     t->sorted_codes = kin;
     t->order = vin;
+    return NB_OK;
+}
+
+// Root cube, 63-bit codes and the stable LSD sort of the code bits
+// [first_shift, 64) (first_shift 0: the full code).  Leaves the sorted codes
+// and the permutation (sorted index -> original index) in t.
+static nb_status morton_sort(BHTree *t, const double *x, const double *y, const double *z,
+                             int n, int first_shift, cudaStream_t st, bool hilbert = false)
+{
+    const int nparts = std::min(div_up(n, 1024), 4 * device_props().num_sms);
+    NB_TRY(t->part.reserve(sizeof(double) * 6 * nparts));
+    NB_TRY(t->root.reserve(sizeof(BHRoot)));
+    NB_TRY(reserve_sort(t, n));
+    BHRoot *root = t->root.as<BHRoot>();
+
+    bbox_partial_kernel<<<nparts, 256, 0, st>>>(x, y, z, n, t->part.as<double>());
+    NB_LAUNCH_CHECK();
+    bbox_final_kernel<<<1, 256, 0, st>>>(t->part.as<double>(), nparts, root);
+    NB_LAUNCH_CHECK();
+    if (hilbert)
+        hilbert_kernel<<<div_up(n, 256), 256, 0, st>>>(x, y, z, n, root, t->keys0.as<uint64_t>(),
+                                                        t->vals0.as<uint32_t>());
+    else
+        encode_kernel<<<div_up(n, 256), 256, 0, st>>>(x, y, z, n, root,
+                                                       t->keys0.as<uint64_t>(),
+                                                       t->vals0.as<uint32_t>());
+    NB_LAUNCH_CHECK();
+    return radix_passes(t, n, first_shift, st);
+}
+
+nb_status bh_sort_buffers(BHTree *t, int n, uint64_t **keys, uint32_t **vals)
+{
+    NB_TRY(reserve_sort(t, std::max(n, 1)));
+    *keys = t->keys0.as<uint64_t>();
+    *vals = t->vals0.as<uint32_t>();
+    return NB_OK;
+}
+
+nb_status bh_sort_keys(BHTree *t, int n, int first_shift, cudaStream_t st,
+                       const uint32_t **order)
+{
+    if (n > 0) NB_TRY(radix_passes(t, n, first_shift, st));
+    *order = t->order;
+    t->tree_valid = false;
     return NB_OK;
 }
 

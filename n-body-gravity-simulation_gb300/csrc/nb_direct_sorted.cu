@@ -58,8 +58,6 @@ namespace nb {
 namespace {
 
 constexpr int kChunk = 32;             // j-chunk = one body per lane
-constexpr float kFarFactor2 = 0.015625f; // (gap / D)^2 threshold: kFarFactor = 1/8
-constexpr float kVeryFar2 = 0.0625f;     // (gap / D)^2 threshold without Newton: 1/4
 constexpr int kResortEvals = 8;        // force evaluations per re-sort
 constexpr bool kHilbertOrder = true;   // sort along the Hilbert curve (else Morton)
 
@@ -104,32 +102,6 @@ __global__ void chunk_box_kernel(const float4 *__restrict__ hi, int n, int nchun
         box[2 * t] = make_float4(mn[0], mn[1], mn[2], 0.f);
         box[2 * t + 1] = make_float4(mx[0], mx[1], mx[2], 0.f);
     }
-}
-
-// s + e = a + b exactly (Knuth's two-sum; plain adds, nothing to contract).
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
-{
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-
-// (h + l) - c as a normalised double-single S + E (|E| <= ulp(S) / 2); the
-// only rounding is that of the low-order add, ~2^-48 |h|.
-__device__ __forceinline__ void rel_ds(float h, float l, float c, float &S, float &E)
-{
-    float s, e;
-    two_sum(h, -c, s, e);
-    two_sum(s, e + l, S, E);
-}
-
-// (h + l) - c rounded to FP32: the S of rel_ds (one rounding of the exact
-// difference, up to the ~2^-48 |h| of the low-order add) without the E.
-__device__ __forceinline__ float rel_s(float h, float l, float c)
-{
-    float s, e;
-    two_sum(h, -c, s, e);
-    return s + (e + l);
 }
 
 // One warp = 32*IPT consecutive sorted i-bodies (chunks tile0 .. tile0+IPT-1,

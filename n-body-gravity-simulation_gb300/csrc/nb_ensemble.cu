@@ -4,9 +4,15 @@
 // all systems is concatenated (system order) in one set of FP64 planes; the
 // forces of every system come from one persistent launch over a per-system
 // work queue (nb_batch.cu); the per-body integrator updates run once over the
-// concatenation; the whole step loop is captured in a CUDA graph and replayed.
-// i-bodies per lane are autotuned per N bucket on the loaded systems before the
-// first evaluation.
+// concatenation; the step loop is captured in a CUDA graph and replayed.
+//
+// By default the force launch is the Hilbert-sorted near/far variant: every
+// system is sorted along a Hilbert curve through its own cube at the start of
+// each nb_ensemble_step call and every kGraphChunk steps (between graph
+// replays, the same points whether or not the steps are replayed), and far
+// j-chunks of an i-chunk take the plain FP32 term.  NB_FLAG_MIXED_UNSORTED
+// selects the all-pairs double-single kernel, whose i-bodies per lane are
+// autotuned per N bucket before the first evaluation.
 #include "nb_internal.h"
 
 #include <algorithm>
@@ -42,6 +48,10 @@ struct nb_ensemble {
     bool profiling = false;
     std::vector<nb::KernelTimer> timers;
     size_t timers_used = 0;
+
+    bool sorted = true;  // the Hilbert-sorted near/far force launch
+    nb::BatchSorted sb;
+    int num_chunks = 0;
 };
 
 namespace nb {
@@ -85,6 +95,12 @@ nb_status ens_force(nb_ensemble *e, const double *px, const double *py, const do
 {
     const int n = (int)e->total;
     float4 *hi = e->hi.as<float4>(), *lo = e->lo.as<float4>();
+    if (e->sorted)
+        return batch_sorted_forces(e->sb, px, py, pz, e->f[9], e->d_sys.as<SysDesc>(),
+                                   e->d_items.as<WorkItem>(), e->num_items,
+                                   e->d_counter.as<int>(), e->cfg.G,
+                                   e->cfg.softening * e->cfg.softening, hi, lo, ax, ay, az,
+                                   e->stream, ens_timer(e, capturing));
     NB_TRY(split_positions(px, py, pz, e->f[9], n, hi, lo, e->stream));
     const double eps2 = e->cfg.softening * e->cfg.softening;
     return batch_forces(hi, lo, e->d_sys.as<SysDesc>(), e->d_items.as<WorkItem>(), e->num_items,
@@ -156,10 +172,29 @@ nb_status step_direct(nb_ensemble *e, int integ, double dt, bool capturing)
     return integrate_step(integ, (int)e->total, dt, e->f, b, e->forces_valid, force, e->stream);
 }
 
+// The sorted path's tables (its shape is fixed: one 32-body i-chunk per item).
+nb_status setup_sorted(nb_ensemble *e)
+{
+    for (const SysDesc &sd : e->sys) e->ipt_bucket[bucket_of(sd.n)] = sd.ipt;
+    NB_TRY(upload_items(e));
+    NB_TRY(batch_sorted_setup(e->sb, e->d_sys.as<SysDesc>(), e->num_sys, e->num_chunks,
+                              (int)e->total, e->stream));
+    e->tuned = true;
+    return NB_OK;
+}
+
+// Every system's order from the current positions (sorted path only).
+nb_status sort_systems(nb_ensemble *e)
+{
+    if (!e->sorted) return NB_OK;
+    return batch_sorted_sort(e->sb, e->d_sys.as<SysDesc>(), e->f[0], e->f[1], e->f[2],
+                             e->stream);
+}
+
 nb_status ready(nb_ensemble *e)
 {
     if (!e->loaded) return fail(NB_ERR_NOT_LOADED, "ensemble: nothing loaded");
-    if (!e->tuned) NB_TRY(tune(e));
+    if (!e->tuned) NB_TRY(e->sorted ? setup_sorted(e) : tune(e));
     return NB_OK;
 }
 
@@ -219,6 +254,8 @@ nb_status nb_ensemble_create(const nb_config *cfg, int num_systems, const int *s
         e->sys[s] = SysDesc{(int)first, sizes[s], 1, 0};
         first += sizes[s];
     }
+    e->sorted = (cfg->flags & NB_FLAG_MIXED_UNSORTED) == 0;
+    if (e->sorted) e->num_chunks = batch_sorted_chunks(e->sys);
     *out = e;
     return NB_OK;
 }
@@ -235,6 +272,7 @@ nb_status nb_ensemble_destroy(nb_ensemble *e)
     nb::DevBuf *bufs[] = {&e->state, &e->hi, &e->lo, &e->old_acc, &e->rk4, &e->d_sys,
                           &e->d_items, &e->d_counter};
     for (nb::DevBuf *b : bufs) b->release();
+    e->sb.release();
     if (e->own_stream) cudaStreamDestroy(e->stream);
     delete e;
     return NB_OK;
@@ -282,7 +320,7 @@ nb_status nb_ensemble_tune(nb_ensemble *e, int *ipt_by_bucket)
         cudaGraphExecDestroy(e->graph);
         e->graph = nullptr;
     }
-    NB_TRY(tune(e));
+    NB_TRY(e->sorted ? setup_sorted(e) : tune(e));
     if (ipt_by_bucket)
         for (int b = 0; b < 32; ++b) ipt_by_bucket[b] = e->ipt_bucket[b];
     return NB_OK;
@@ -292,6 +330,7 @@ nb_status nb_ensemble_compute_forces(nb_ensemble *e)
 {
     if (!e) return fail(NB_ERR_INVALID_ARGUMENT, "ensemble is NULL");
     NB_TRY(ready(e));
+    NB_TRY(sort_systems(e));
     NB_TRY(ens_force(e, e->f[0], e->f[1], e->f[2], e->f[6], e->f[7], e->f[8], false));
     e->forces_valid = true;
     return NB_OK;
@@ -308,6 +347,9 @@ nb_status nb_ensemble_step(nb_ensemble *e, int integrator, double dt, int nsteps
     if (integrator == NB_VELOCITY_VERLET) NB_TRY(e->old_acc.reserve(sizeof(double) * 3 * e->ps));
     if (integrator == NB_RK4) NB_TRY(e->rk4.reserve(sizeof(double) * 27 * e->ps));
     int done = 0;
+    // the sorted path re-sorts here and every `chunk` steps after the first
+    // replay's start: the same points for replayed and for direct steps
+    NB_TRY(sort_systems(e));
     // Leapfrog / Verlet need a valid start-of-step force before the loop is
     // captured, so that every captured step is the same sequence.
     if ((integrator == NB_LEAPFROG || integrator == NB_VELOCITY_VERLET) && !e->forces_valid &&
@@ -317,43 +359,47 @@ nb_status nb_ensemble_step(nb_ensemble *e, int integrator, double dt, int nsteps
     }
     const int remaining = nsteps - done;
     const int chunk = std::min(kGraphChunk, remaining);
-    if (chunk >= 2 && !e->profiling) {
-        if (!e->graph || e->graph_integ != integrator || e->graph_dt != dt ||
-            e->graph_steps != chunk) {
-            if (e->graph) {
-                cudaGraphExecDestroy(e->graph);
-                e->graph = nullptr;
-            }
-            bool valid_before = e->forces_valid;
-            NB_CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-            nb_status cs = NB_OK;
-            for (int k = 0; k < chunk && cs == NB_OK; ++k) cs = step_direct(e, integrator, dt, true);
-            cudaGraph_t g = nullptr;
-            cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
-            e->forces_valid = valid_before;
-            if (cs != NB_OK) {
-                if (g) cudaGraphDestroy(g);
-                return cs;
-            }
-            if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
-            ce = cudaGraphInstantiate(&e->graph, g, 0);
-            cudaGraphDestroy(g);
-            if (ce != cudaSuccess) {
-                e->graph = nullptr;
-                return cuda_fail(ce, "cudaGraphInstantiate");
-            }
-            e->graph_integ = integrator;
-            e->graph_dt = dt;
-            e->graph_steps = chunk;
+    const int launches = chunk >= 2 ? remaining / chunk : 0;
+    const bool use_graph = launches > 0 && !e->profiling;
+    if (use_graph && (!e->graph || e->graph_integ != integrator || e->graph_dt != dt ||
+                      e->graph_steps != chunk)) {
+        if (e->graph) {
+            cudaGraphExecDestroy(e->graph);
+            e->graph = nullptr;
         }
-        const int launches = remaining / chunk;
-        for (int k = 0; k < launches; ++k) {
+        bool valid_before = e->forces_valid;
+        NB_CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+        nb_status cs = NB_OK;
+        for (int k = 0; k < chunk && cs == NB_OK; ++k) cs = step_direct(e, integrator, dt, true);
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+        e->forces_valid = valid_before;
+        if (cs != NB_OK) {
+            if (g) cudaGraphDestroy(g);
+            return cs;
+        }
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+        ce = cudaGraphInstantiate(&e->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            e->graph = nullptr;
+            return cuda_fail(ce, "cudaGraphInstantiate");
+        }
+        e->graph_integ = integrator;
+        e->graph_dt = dt;
+        e->graph_steps = chunk;
+    }
+    for (int k = 0; k < launches; ++k) {
+        if (k > 0) NB_TRY(sort_systems(e));
+        if (use_graph) {
             NB_CUDA_TRY(cudaGraphLaunch(e->graph, e->stream));
             ++e->graph_launches;
+            // a replayed chunk leaves the force valid exactly as direct steps would
+            e->forces_valid = (integrator == NB_LEAPFROG || integrator == NB_VELOCITY_VERLET);
+        } else {
+            for (int c = 0; c < chunk; ++c) NB_TRY(step_direct(e, integrator, dt, false));
         }
-        // the replayed steps leave the force valid exactly as a direct step would
-        e->forces_valid = (integrator == NB_LEAPFROG || integrator == NB_VELOCITY_VERLET);
-        done += launches * chunk;
+        done += chunk;
     }
     for (; done < nsteps; ++done) NB_TRY(step_direct(e, integrator, dt, false));
     return NB_OK;

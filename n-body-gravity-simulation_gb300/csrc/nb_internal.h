@@ -92,6 +92,13 @@ DirectPlan direct_mixed_plan(int n);
 // j-split count filling whole waves of `slots` resident CTAs.
 int direct_pick_segments(int iblocks, int tiles, int slots);
 
+// Thresholds of the sorted near/far kernels as (gap / D)^2, D the diameter of
+// a warp's i-box: a j-chunk at least D/8 away takes the plain FP32 term, one
+// at least D/4 away also drops the Newton step (kFarFactor = 1/8, kVeryFar =
+// 1/4).
+constexpr float kFarFactor2 = 0.015625f;
+constexpr float kVeryFar2 = 0.0625f;
+
 // Hilbert-sorted near/far variant of the mixed path (nb_direct_sorted.cu).
 struct BHTree;
 struct SortedBuffers {
@@ -177,7 +184,7 @@ struct SysDesc {
     int first;
     int n;
     int ipt;
-    int pad;
+    int chunk0;  // first 32-body chunk of the system (the sorted batch path)
 };
 // One queue item: i-bodies [i0, i0 + 32 * ipt) of system `sys`.
 struct WorkItem {
@@ -185,6 +192,35 @@ struct WorkItem {
     int i0;
 };
 int bucket_of(int n);  // floor(log2(n))
+// Hilbert-sorted variant of the batched forces (nb_batch.cu): each system's
+// bodies are sorted along a Hilbert curve through its own cube; an item is one
+// or two 32-body i-chunks; j-chunks far from its box take the plain FP32 term.
+struct BHTree;
+struct BatchSorted {
+    BHTree *sorter = nullptr;
+    DevBuf body_sys, chunks, geom, boxes;
+    const uint32_t *order = nullptr;  // sorted index -> body (sorter-owned)
+    int num_sys = 0, num_chunks = 0, total = 0, key_shift = 0, first_shift = 0;
+    void release();
+};
+// i-chunks per warp item of an n-body system in the sorted variant (1 or 2).
+int batch_sorted_ipt(int n);
+// Sets every system's ipt (batch_sorted_ipt) and chunk0; returns the chunk count.
+int batch_sorted_chunks(std::vector<SysDesc> &sys);
+// Device tables for the systems of d_sys (already uploaded with chunk0).
+nb_status batch_sorted_setup(BatchSorted &b, const SysDesc *d_sys, int num_sys, int num_chunks,
+                             int total, cudaStream_t st);
+// (Re)computes the order from the positions x, y, z.
+nb_status batch_sorted_sort(BatchSorted &b, const SysDesc *d_sys, const double *x,
+                            const double *y, const double *z, cudaStream_t st);
+// a = G sum_j ... for every body, in the order of the last sort (hi/lo are
+// scratch mirrors of total entries).
+nb_status batch_sorted_forces(BatchSorted &b, const double *x, const double *y, const double *z,
+                              const double *m, const SysDesc *d_sys, const WorkItem *d_items,
+                              int num_items, int *d_counter, double G, double eps2, float4 *hi,
+                              float4 *lo, double *ax, double *ay, double *az, cudaStream_t st,
+                              const KernelTimer *timer);
+
 // Items of every system, largest cost first.
 void build_work_items(const std::vector<SysDesc> &sys, std::vector<WorkItem> &items);
 // Mixed-precision forces of all systems of the queue (persistent kernel).
@@ -221,6 +257,13 @@ nb_status bh_morton_order(BHTree *t, const double *x, const double *y, const dou
 // the root cube (runs of sorted bodies fill compact regions).
 nb_status bh_hilbert_order(BHTree *t, const double *x, const double *y, const double *z, int n,
                            cudaStream_t st, const uint32_t **order, const double **root_centre);
+// A stable sort of caller-made keys: bh_sort_buffers returns the key and
+// value arrays (n entries) to fill on the device; bh_sort_keys then sorts them
+// by the key bits [first_shift, 64) and returns the sorted values (valid until
+// the next call on t).
+nb_status bh_sort_buffers(BHTree *t, int n, uint64_t **keys, uint32_t **vals);
+nb_status bh_sort_keys(BHTree *t, int n, int first_shift, cudaStream_t st,
+                       const uint32_t **order);
 nb_status bh_read_order(BHTree *t, cudaStream_t st, uint64_t *codes, uint32_t *order);
 nb_status bh_read_nodes(BHTree *t, cudaStream_t st, int max_nodes, int *depth,
                         uint64_t *prefix, int *first, int *count, int *is_leaf, int *skip,

@@ -47,6 +47,32 @@ __device__ __forceinline__ void ds_add_kahan(float &hi, float &lo, float s, floa
     lo = lo + (e - c);
 }
 
+// s + e = a + b exactly (Knuth's two-sum; plain adds, nothing to contract).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// (h + l) - c as a normalised double-single S + E (|E| <= ulp(S) / 2); the
+// only rounding is that of the low-order add, ~2^-48 |h|.
+__device__ __forceinline__ void rel_ds(float h, float l, float c, float &S, float &E)
+{
+    float s, e;
+    two_sum(h, -c, s, e);
+    two_sum(s, e + l, S, E);
+}
+
+// (h + l) - c rounded to FP32: the S of rel_ds (one rounding of the exact
+// difference, up to the ~2^-48 |h| of the low-order add) without the E.
+__device__ __forceinline__ float rel_s(float h, float l, float c)
+{
+    float s, e;
+    two_sum(h, -c, s, e);
+    return s + (e + l);
+}
+
 // a += m_j (r_j - r_i) / (|r_j - r_i|^2 + eps2)^(3/2) for one (i, j) pair.
 // ZERO_SOFT: eps2 == 0, where the j == i term (r2 == 0) must give 0.
 template <bool ZERO_SOFT>

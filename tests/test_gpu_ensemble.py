@@ -19,13 +19,19 @@ def make(nb, num, lo=32, hi=4096, seed=3):
     return sizes, nb.plummer_ensemble(sizes, seed=seed * 1000)
 
 
-def cfg(nb, eps=1e-2):
-    return nb.Config(method=nb.DIRECT_MIXED, G=1.0, softening=eps)
+def cfg(nb, eps=1e-2, flags=0):
+    return nb.Config(method=nb.DIRECT_MIXED, G=1.0, softening=eps, flags=flags)
 
 
-def test_forces_match_oracle(nb, oracle):
+KERNELS = {"sorted": 0, "unsorted": 8}  # default / NB_FLAG_MIXED_UNSORTED
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_forces_match_oracle(nb, oracle, kernel):
+    """Both force launches: the default Hilbert-sorted near/far one and the
+    all-pairs double-single one (NB_FLAG_MIXED_UNSORTED)."""
     sizes, st = make(nb, 40)
-    with nb.Ensemble(cfg(nb), sizes) as e:
+    with nb.Ensemble(cfg(nb, flags=KERNELS[kernel]), sizes) as e:
         e.load(*st)
         e.compute_forces()
         got = e.read_state()
@@ -44,16 +50,17 @@ def test_forces_match_oracle(nb, oracle):
         assert (d / r)[well].max(initial=0.0) <= TOL, s
 
 
-def test_system_alone_equals_in_mix(nb):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_system_alone_equals_in_mix(nb, kernel):
     sizes, st = make(nb, 30, seed=5)
-    with nb.Ensemble(cfg(nb), sizes) as e:
+    with nb.Ensemble(cfg(nb, flags=KERNELS[kernel]), sizes) as e:
         e.load(*st)
         e.step(nb.RK4, 1e-3, 7)
         mix = e.read_state()
     for s in (0, 11, 29):
         a, b = int(np.sum(sizes[:s])), int(np.sum(sizes[:s + 1]))
         one = tuple(v[a:b] for v in st)
-        with nb.Ensemble(cfg(nb), [sizes[s]]) as e1:
+        with nb.Ensemble(cfg(nb, flags=KERNELS[kernel]), [sizes[s]]) as e1:
             e1.load(*one)
             e1.step(nb.RK4, 1e-3, 7)
             alone = e1.read_state()
@@ -61,14 +68,17 @@ def test_system_alone_equals_in_mix(nb):
             assert np.array_equal(alone[k], mix[k][a:b]), (s, k)
 
 
-def test_graph_replay_equals_direct_launches(nb):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_graph_replay_equals_direct_launches(nb, kernel):
+    """60 steps: two replayed 25-step chunks (the sorted kernel re-sorts
+    before the second) and 10 direct steps, against 60 direct steps."""
     sizes, st = make(nb, 20, seed=6)
     out = []
     for profile in (False, True):  # profiling runs the steps without the graph
-        with nb.Ensemble(cfg(nb), sizes) as e:
+        with nb.Ensemble(cfg(nb, flags=KERNELS[kernel]), sizes) as e:
             e.load(*st)
             e.profile(profile)
-            e.step(nb.RK4, 1e-3, 30)
+            e.step(nb.RK4, 1e-3, 60)
             out.append(e.read_state())
             info = e.info()
             if not profile:
