@@ -476,6 +476,13 @@ const char *nb_version(void);
  * then disarms.  A negative value disarms it. */
 nb_status nb_debug_fail_device_allocations(int after);
 
+/* Device-side index checks.  *enabled (if not NULL) is 1 in a library built
+ * with them (build.py --checks: every kernel tests the indices it is about to
+ * use and skips an out-of-range access instead of making it), else 0.  Returns
+ * NB_ERR_DEVICE_FAULT with the source line, index and bound of the first
+ * failed check since the last call (and clears them), else NB_OK. */
+nb_status nb_debug_device_checks(int *enabled);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,6 +20,7 @@
 // ipt (i-bodies per lane) is chosen per N bucket (powers of two) by an
 // autotuner that times the candidates on the batch's own systems.
 #include "nb_internal.h"
+#include "nb_check.cuh"
 #include "nb_curve.cuh"
 #include "nb_pair.cuh"
 
@@ -105,7 +106,8 @@ __global__ void __launch_bounds__(kBatchBlock)
 batch_force_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                    const SysDesc *__restrict__ sys, const WorkItem *__restrict__ items,
                    int num_items, int *__restrict__ counter, float eps2, double G,
-                   double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az)
+                   double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
+                   int total)
 {
     __shared__ PairTile tiles[kBatchWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -116,6 +118,7 @@ batch_force_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
         if (item >= num_items) break;
         const WorkItem w = items[item];
         const SysDesc sd = sys[w.sys];
+        if (!NB_IN_RANGE(sd.first, total) || !NB_IN_RANGE(sd.first + sd.n - 1, total)) continue;
         switch (sd.ipt) {
         case 1:
             batch_item<1, ZERO_SOFT>(hi, lo, sd, w.i0, eps2, G, ax, ay, az,
@@ -253,6 +256,7 @@ batch_split_sorted_kernel(const uint32_t *__restrict__ order, const double *__re
     const int i = blockIdx.x * 256 + threadIdx.x;
     if (i >= n) return;
     const uint32_t o = order[i];
+    if (!NB_IN_RANGE(o, n)) return;
     const double4 g = geom[body_sys[i]];
     const double X = x[o] - g.x, Y = y[o] - g.y, Z = z[o] - g.z;
     const float hx = __double2float_rn(X), hy = __double2float_rn(Y), hz = __double2float_rn(Z);
@@ -299,7 +303,8 @@ __device__ __forceinline__ void batch_sorted_item(const float4 *__restrict__ hi,
                                                   double G, const uint32_t *__restrict__ order,
                                                   double *__restrict__ ax,
                                                   double *__restrict__ ay,
-                                                  double *__restrict__ az, PairTile &sg)
+                                                  double *__restrict__ az, PairTile &sg,
+                                                  int total)
 {
     const int lane = threadIdx.x & 31;
     const int nch = (sd.n + 31) / 32;
@@ -421,6 +426,7 @@ __device__ __forceinline__ void batch_sorted_item(const float4 *__restrict__ hi,
         const int i = i0 + 32 * k + lane;
         if (i < sd.n) {
             const uint32_t o = order[sd.first + i];
+            if (!NB_IN_RANGE(o, total)) continue;
             ax[o] = G * ((double)sx[k] - (double)qx[k]);
             ay[o] = G * ((double)sy[k] - (double)qy[k]);
             az[o] = G * ((double)sz[k] - (double)qz[k]);
@@ -434,7 +440,8 @@ batch_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo
                     const float4 *__restrict__ box, const SysDesc *__restrict__ sys,
                     const WorkItem *__restrict__ items, int num_items, int *__restrict__ counter,
                     float eps2, double G, const uint32_t *__restrict__ order,
-                    double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az)
+                    double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
+                    int total, int num_chunks)
 {
     __shared__ PairTile tiles[kBatchWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -445,12 +452,15 @@ batch_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo
         if (item >= num_items) break;
         const WorkItem w = items[item];
         const SysDesc sd = sys[w.sys];
+        if (!NB_IN_RANGE(sd.first, total) || !NB_IN_RANGE(sd.first + sd.n - 1, total) ||
+            !NB_IN_RANGE(sd.chunk0 + (sd.n - 1) / 32, num_chunks))
+            continue;
         if (sd.ipt == 2)
             batch_sorted_item<2, ZERO_SOFT>(hi, lo, box, sd, w.i0, eps2, G, order, ax, ay, az,
-                                            tiles[warp]);
+                                            tiles[warp], total);
         else
             batch_sorted_item<1, ZERO_SOFT>(hi, lo, box, sd, w.i0, eps2, G, order, ax, ay, az,
-                                            tiles[warp]);
+                                            tiles[warp], total);
     }
 }
 
@@ -495,18 +505,18 @@ void build_work_items(const std::vector<SysDesc> &sys, std::vector<WorkItem> &it
 
 nb_status batch_forces(const float4 *hi, const float4 *lo, const SysDesc *d_sys,
                        const WorkItem *d_items, int num_items, int *d_counter, double G,
-                       double eps2, double *ax, double *ay, double *az, cudaStream_t st,
-                       const KernelTimer *timer)
+                       double eps2, double *ax, double *ay, double *az, int total,
+                       cudaStream_t st, const KernelTimer *timer)
 {
     if (num_items <= 0) return NB_OK;
     NB_CUDA_TRY(cudaMemsetAsync(d_counter, 0, sizeof(int), st));
     if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
     if (eps2 > 0.0)
         batch_force_kernel<false><<<batch_grid(), kBatchBlock, 0, st>>>(
-            hi, lo, d_sys, d_items, num_items, d_counter, (float)eps2, G, ax, ay, az);
+            hi, lo, d_sys, d_items, num_items, d_counter, (float)eps2, G, ax, ay, az, total);
     else
         batch_force_kernel<true><<<batch_grid(), kBatchBlock, 0, st>>>(
-            hi, lo, d_sys, d_items, num_items, d_counter, 0.0f, G, ax, ay, az);
+            hi, lo, d_sys, d_items, num_items, d_counter, 0.0f, G, ax, ay, az, total);
     NB_LAUNCH_CHECK();
     if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
     return NB_OK;
@@ -590,11 +600,11 @@ nb_status batch_sorted_forces(BatchSorted &b, const double *x, const double *y, 
     if (eps2 > 0.0)
         batch_sorted_kernel<false><<<batch_sorted_grid(), kBatchBlock, 0, st>>>(
             hi, lo, b.boxes.as<float4>(), d_sys, d_items, num_items, d_counter, (float)eps2, G,
-            b.order, ax, ay, az);
+            b.order, ax, ay, az, b.total, b.num_chunks);
     else
         batch_sorted_kernel<true><<<batch_sorted_grid(), kBatchBlock, 0, st>>>(
             hi, lo, b.boxes.as<float4>(), d_sys, d_items, num_items, d_counter, 0.0f, G,
-            b.order, ax, ay, az);
+            b.order, ax, ay, az, b.total, b.num_chunks);
     NB_LAUNCH_CHECK();
     if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
     return NB_OK;

@@ -40,6 +40,7 @@
 // num_nodes steps: there is no stack to overflow.  Accelerations are scattered
 // back to the original order in FP64, multiplied by G.
 #include "nb_internal.h"
+#include "nb_check.cuh"
 #include "nb_curve.cuh"
 #include "nb_pair.cuh"
 
@@ -405,6 +406,7 @@ radix_scatter_kernel(const uint64_t *__restrict__ kin, const uint32_t *__restric
         const uint64_t k = skey[j];
         const int d = (int)((k >> shift) & 0xFF);
         const int pos = toff[d] + (j - tstart[d]);
+        if (!NB_IN_RANGE(pos, n)) continue;
         kout[pos] = k;
         vout[pos] = sval[j];
     }
@@ -420,6 +422,7 @@ gather_kernel(const uint32_t *__restrict__ order, const double *__restrict__ x,
     const int i = blockIdx.x * 256 + threadIdx.x;
     if (i >= n) return;
     const uint32_t o = order[i];
+    if (!NB_IN_RANGE(o, n)) return;
     const double rx = x[o] - root->cx, ry = y[o] - root->cy, rz = z[o] - root->cz;
     const double mm = m[o];
     body[i] = make_float4((float)rx, (float)ry, (float)rz, (float)mm);
@@ -680,7 +683,7 @@ node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__rest
             const int *__restrict__ chain_len, const int *__restrict__ chain_depth,
             const int *__restrict__ offsets, const D4 *__restrict__ P,
             BHNode *__restrict__ nodes, unsigned char *__restrict__ node_depth,
-            BHStats *__restrict__ stats)
+            BHStats *__restrict__ stats, int node_cap)
 {
     const int i = blockIdx.x * 256 + threadIdx.x;
     if (i >= n) return;
@@ -694,6 +697,7 @@ node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__rest
         const int d = a + k;
         const int cnt = cell_end(c, n, i, d) - i;
         const bool leaf = !(cnt > cap && d < levels);
+        if (!NB_IN_RANGE(id0 + k, node_cap) || !NB_IN_RANGE(i + cnt, n + 1)) break;
         BHNode nd;
         nd.com_mass = monopole(P[i], P[i + cnt]);
         nd.first = i;
@@ -842,7 +846,9 @@ walk_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
                 continue;
             }
             // leaf: its bodies, two per f32x2 instruction
-            const int e = nd.first + nd.count;
+            const int e = NB_IN_RANGE(nd.first, n) && NB_IN_RANGE(nd.first + nd.count - 1, n)
+                              ? nd.first + nd.count
+                              : nd.first;
             int b = nd.first;
             for (; b + 1 < e; b += 2) {
                 const float4 q0 = body[b], q1 = body[b + 1];
@@ -893,6 +899,7 @@ walk_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
             }
             ++m2p;
         }
+        if (!NB_IN_RANGE(nd.skip - node - 1, num_nodes)) break;  // skips only go forward
         node = nd.skip;
     }
     if (valid) {
@@ -968,7 +975,9 @@ walk2_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
                 ++node;
                 continue;
             }
-            const int e = nd.first + nd.count;
+            const int e = NB_IN_RANGE(nd.first, n) && NB_IN_RANGE(nd.first + nd.count - 1, n)
+                              ? nd.first + nd.count
+                              : nd.first;
             for (int b = nd.first; b < e; ++b) {
                 const float4 q = body[b];
 #pragma unroll
@@ -1021,6 +1030,7 @@ walk2_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
             }
             ++m2p;
         }
+        if (!NB_IN_RANGE(nd.skip - node - 1, num_nodes)) break;  // skips only go forward
         node = nd.skip;
     }
     unsigned nv = 0;
@@ -1423,7 +1433,8 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
                                                 t->chain_len.as<int>(), t->chain_depth.as<int>(),
                                                 t->offsets.as<int>(), t->prefix.as<D4>(),
                                                 t->nodes.as<BHNode>(),
-                                                t->node_depth.as<unsigned char>(), stats);
+                                                t->node_depth.as<unsigned char>(), stats,
+                                                t->node_cap);
     NB_LAUNCH_CHECK();
     if (quad) NB_TRY(compute_quads(t, x, y, z, m, n, st));
     t->tree_valid = true;

@@ -46,6 +46,7 @@
 // accumulator takes 16 terms before its Kahan-compensated add, and the
 // segments combine as a double-single.
 #include "nb_internal.h"
+#include "nb_check.cuh"
 #include "nb_pair.cuh"
 
 #include <algorithm>
@@ -72,6 +73,7 @@ __global__ void split_sorted_kernel(const uint32_t *__restrict__ order,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t o = order[i];
+    if (!NB_IN_RANGE(o, n)) return;
     const double X = x[o] - centre[0], Y = y[o] - centre[1], Z = z[o] - centre[2];
     const float hx = __double2float_rn(X), hy = __double2float_rn(Y), hz = __double2float_rn(Z);
     hi[i] = make_float4(hx, hy, hz, __double2float_rn(m[o]));
@@ -284,6 +286,7 @@ __global__ void combine_sorted_kernel(const float *__restrict__ psum,
             ds_add_kahan(hi[c], lo[c], psum[base + c * plane + i], pcomp[base + c * plane + i]);
     }
     const uint32_t o = order[i];
+    if (!NB_IN_RANGE(o, n)) return;
     ax[o] = G * ((double)hi[0] + (double)lo[0]);
     ay[o] = G * ((double)hi[1] + (double)lo[1]);
     az[o] = G * ((double)hi[2] + (double)lo[2]);

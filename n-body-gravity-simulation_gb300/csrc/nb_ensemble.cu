@@ -104,7 +104,7 @@ nb_status ens_force(nb_ensemble *e, const double *px, const double *py, const do
     NB_TRY(split_positions(px, py, pz, e->f[9], n, hi, lo, e->stream));
     const double eps2 = e->cfg.softening * e->cfg.softening;
     return batch_forces(hi, lo, e->d_sys.as<SysDesc>(), e->d_items.as<WorkItem>(), e->num_items,
-                        e->d_counter.as<int>(), e->cfg.G, eps2, ax, ay, az, e->stream,
+                        e->d_counter.as<int>(), e->cfg.G, eps2, ax, ay, az, n, e->stream,
                         ens_timer(e, capturing));
 }
 
@@ -133,12 +133,12 @@ nb_status tune(nb_ensemble *e)
             // warm, then two timed launches into the real acceleration planes
             NB_TRY(batch_forces(hi, lo, e->d_sys.as<SysDesc>(), e->d_items.as<WorkItem>(),
                                 e->num_items, e->d_counter.as<int>(), e->cfg.G, eps2, e->f[6],
-                                e->f[7], e->f[8], e->stream));
+                                e->f[7], e->f[8], n, e->stream));
             NB_CUDA_TRY(cudaEventRecord(t0, e->stream));
             for (int r = 0; r < 2; ++r)
                 NB_TRY(batch_forces(hi, lo, e->d_sys.as<SysDesc>(), e->d_items.as<WorkItem>(),
                                     e->num_items, e->d_counter.as<int>(), e->cfg.G, eps2,
-                                    e->f[6], e->f[7], e->f[8], e->stream));
+                                    e->f[6], e->f[7], e->f[8], n, e->stream));
             NB_CUDA_TRY(cudaEventRecord(t1, e->stream));
             NB_CUDA_TRY(cudaEventSynchronize(t1));
             float ms = 0.f;

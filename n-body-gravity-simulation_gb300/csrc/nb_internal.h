@@ -51,6 +51,18 @@ struct NvtxRange {
     NvtxRange &operator=(const NvtxRange &) = delete;
 };
 
+// The first failed device-side index check of a translation unit of a
+// checked build (nb_check.cuh): source line, index and bound.
+struct DeviceCheck {
+    int failed;
+    int line;
+    long long index;
+    long long bound;
+};
+using CheckReader = nb_status (*)(DeviceCheck *out, bool clear);
+// Called by every checked translation unit at load time.
+void register_check_reader(const char *file, CheckReader reader);
+
 // ---------------------------------------------------------------- memory
 // A device buffer that grows on demand and is freed with its owner.
 struct DevBuf {
@@ -226,8 +238,8 @@ void build_work_items(const std::vector<SysDesc> &sys, std::vector<WorkItem> &it
 // Mixed-precision forces of all systems of the queue (persistent kernel).
 nb_status batch_forces(const float4 *hi, const float4 *lo, const SysDesc *d_sys,
                        const WorkItem *d_items, int num_items, int *d_counter, double G,
-                       double eps2, double *ax, double *ay, double *az, cudaStream_t st,
-                       const KernelTimer *timer = nullptr);
+                       double eps2, double *ax, double *ay, double *az, int total,
+                       cudaStream_t st, const KernelTimer *timer = nullptr);
 
 // ---------------------------------------------------------------- Barnes-Hut
 struct BHTree;  // opaque, defined in nb_bh.cu

@@ -392,7 +392,7 @@ nb_status tick(nb_server *s)
             NB_TRY(split_positions(s->f[0], s->f[1], s->f[2], s->f[9], hw, hi, lo, s->stream));
             NB_TRY(batch_forces(hi, lo, s->d_new_sys.as<SysDesc>(), s->d_new_items.as<WorkItem>(),
                                 nn, s->d_counter.as<int>(), s->cfg.G, eps2, s->f[6], s->f[7],
-                                s->f[8], s->stream));
+                                s->f[8], hw, s->stream));
         }
         NB_TRY(kick_drift(NB_LEAPFROG, hw, dt, s->f[0], s->f[1], s->f[2], s->f[3], s->f[4],
                           s->f[5], s->f[6], s->f[7], s->f[8], nullptr, nullptr, nullptr,
@@ -400,7 +400,7 @@ nb_status tick(nb_server *s)
         NB_TRY(split_positions(s->f[0], s->f[1], s->f[2], s->f[9], hw, hi, lo, s->stream));
         NB_TRY(batch_forces(hi, lo, s->d_sys.as<SysDesc>(), s->d_items.as<WorkItem>(),
                             s->num_items, s->d_counter.as<int>(), s->cfg.G, eps2, s->f[6],
-                            s->f[7], s->f[8], s->stream));
+                            s->f[7], s->f[8], hw, s->stream));
         NB_TRY(kick(NB_LEAPFROG, hw, dt, s->f[3], s->f[4], s->f[5], s->f[6], s->f[7], s->f[8],
                     nullptr, nullptr, nullptr, s->stream));
         NB_CUDA_TRY(cudaEventRecord(s->direct_done, s->stream));

@@ -17,7 +17,23 @@
 #include <mutex>
 #include <vector>
 
+#ifndef NB_DEVICE_CHECKS
+#define NB_DEVICE_CHECKS 0
+#endif
+#define NB_DEVICE_CHECKS_BUILD NB_DEVICE_CHECKS
+
 namespace nb {
+
+std::vector<std::pair<const char *, CheckReader>> &check_readers()
+{
+    static std::vector<std::pair<const char *, CheckReader>> readers;
+    return readers;
+}
+
+void register_check_reader(const char *file, CheckReader reader)
+{
+    check_readers().emplace_back(file, reader);
+}
 
 namespace {
 thread_local std::string g_last_error;
@@ -615,6 +631,21 @@ const char *nb_status_string(nb_status s)
 const char *nb_last_error(void) { return g_last_error.c_str(); }
 
 const char *nb_version(void) { return "nbody-gb300 0.1 (sm_103a)"; }
+
+nb_status nb_debug_device_checks(int *enabled)
+{
+    if (enabled) *enabled = NB_DEVICE_CHECKS_BUILD;
+    std::string first;
+    for (const auto &r : check_readers()) {
+        DeviceCheck c{};
+        NB_TRY(r.second(&c, true));
+        if (c.failed && first.empty())
+            first = std::string(r.first) + ":" + std::to_string(c.line) + ": index " +
+                    std::to_string(c.index) + " outside [0, " + std::to_string(c.bound) + ")";
+    }
+    if (!first.empty()) return fail(NB_ERR_DEVICE_FAULT, "device check failed at " + first);
+    return NB_OK;
+}
 
 nb_status nb_debug_fail_device_allocations(int after)
 {

@@ -21,7 +21,8 @@ from dataclasses import dataclass
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libnbody_gb300.so")
+# NBODY_GB300_LIB selects another build of the library (the device-checked one)
+LIB_PATH = os.environ.get("NBODY_GB300_LIB") or os.path.join(HERE, "libnbody_gb300.so")
 COMPAT_LIB_PATH = os.path.join(HERE, "libnbody_compat.so")
 
 # nb_method
@@ -50,7 +51,7 @@ EXPORTS = [
     "nb_ensemble_synchronize", "nb_ensemble_info", "nb_ensemble_profile",
     "nb_server_config_default", "nb_server_create", "nb_server_destroy", "nb_server_submit",
     "nb_server_tick", "nb_server_result", "nb_server_release", "nb_server_get_stats",
-    "nb_server_cancel", "nb_debug_fail_device_allocations",
+    "nb_server_cancel", "nb_debug_fail_device_allocations", "nb_debug_device_checks",
 ]
 _NON_STATUS = {"nb_status_string", "nb_last_error", "nb_version", "nb_kernel_launch_count"}
 
@@ -219,6 +220,7 @@ def lib():
     L.nb_server_get_stats.argtypes = [vp, C.POINTER(_ServerStats)]
     L.nb_server_cancel.argtypes = [vp, C.c_int64]
     L.nb_debug_fail_device_allocations.argtypes = [C.c_int]
+    L.nb_debug_device_checks.argtypes = [C.POINTER(C.c_int)]
     for name in EXPORTS:
         f = getattr(L, name)
         if name not in _NON_STATUS:
@@ -630,6 +632,15 @@ def _bh_info_dict(info) -> dict:
 
 def version() -> str:
     return lib().nb_version().decode()
+
+
+def debug_device_checks() -> bool:
+    """nb_debug_device_checks: whether this library checks device indices;
+    raises NBodyError (NB_ERR_DEVICE_FAULT, with the source line, index and
+    bound) if a check failed since the last call."""
+    enabled = C.c_int()
+    _check(lib().nb_debug_device_checks(C.byref(enabled)), "nb_debug_device_checks")
+    return bool(enabled.value)
 
 
 def debug_fail_device_allocations(after: int):

@@ -88,3 +88,9 @@ def test_create_fails_cleanly_without_gpu(nb):
     with pytest.raises(nb.NBodyError) as e:
         nb.Sim(nb.Config(), capacity=16)
     assert e.value.status in (2, 3)  # NB_ERR_CUDA / out of memory: no device
+
+
+def test_normal_build_has_no_device_checks(nb):
+    """nb_debug_device_checks needs no GPU: the normal build reports that its
+    kernels carry no index checks (the checked build is tested on the GPU)."""
+    assert nb.debug_device_checks() is False
