@@ -181,6 +181,33 @@ def test_bench_workload_forces_along_the_trajectory(nb, oracle):
             check_mixed(oracle, (cur["ax"], cur["ay"], cur["az"]), ref, state, G, eps)
 
 
+def test_sorted_kernel_at_2_20_bodies_sampled_rows(nb, oracle):
+    """The default mixed path at N = 2^20 (disk + bulge, the Barnes-Hut
+    workload's bodies): many j-segments, deep chunk tables.  1024 bodies are
+    checked against the oracle's FP64 rows over all 2^20 j, with S_i from an
+    FP64 torch sum on the GPU."""
+    torch = pytest.importorskip("torch")
+    n, G, eps, rows = 1 << 20, 1.0, 1e-3, 1024
+    st = nb.disk_bulge(n, seed=8)
+    a = gpu_forces(nb, nb.DIRECT_MIXED, st, G, eps)
+    x, y, z, m = st[0], st[1], st[2], st[6]
+    ref = oracle.forces_naive_rows(x, y, z, m, G, eps, 0, rows)
+    p = torch.from_numpy(np.stack([x, y, z], 1)).cuda()
+    mm = torch.from_numpy(np.ascontiguousarray(m)).cuda()
+    sabs = np.empty(rows)
+    for i0 in range(0, rows, 16):
+        d = p[None, :, :] - p[i0:i0 + 16, None, :]
+        r2 = (d * d).sum(-1)
+        sabs[i0:i0 + 16] = (mm[None, :] * torch.sqrt(r2) / (r2 + eps * eps) ** 1.5).sum(1).cpu().numpy()
+    got = [v[:rows] for v in a]
+    dd = np.sqrt(sum((u - v) ** 2 for u, v in zip(got, ref)))
+    r = np.sqrt(sum(v * v for v in ref))
+    assert (dd / sabs).max() <= TOL_MIXED
+    well = sabs / r <= KAPPA_WELL
+    assert (dd / r)[well].max() <= TOL_MIXED
+    assert float(np.sqrt(np.mean((dd / r) ** 2))) <= TOL_MIXED_RMS
+
+
 @pytest.mark.parametrize("n", [37, 1000, 3000])
 def test_mixed_sorted_small_and_ragged(nb, oracle, n):
     """The sorted kernel on sizes that are not multiples of its 32-body chunks
