@@ -4,11 +4,12 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 
 namespace nb {
 
 // 21 bits -> every third bit of 63 (standard magic-number spreading).
-__device__ __forceinline__ uint64_t spread21(uint64_t v)
+__host__ __device__ __forceinline__ uint64_t spread21(uint64_t v)
 {
     v &= 0x1fffffull;
     v = (v | v << 32) & 0x1f00000000ffffull;
@@ -20,13 +21,14 @@ __device__ __forceinline__ uint64_t spread21(uint64_t v)
 }
 
 // Position on the Hilbert curve through a 2^10 x 2^10 x 2^10 grid (cells of a
-// cube around the bodies), following J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc.
-// 707 (2004): the grid coordinates are turned into the curve's "transposed"
-// index by reflections and exchanges from the top bit down, Gray-decoded, and
-// their bits interleaved (axis 0 most significant).  Consecutive indices are
+// cube around the bodies), following J. Skilling, "Programming the Hilbert
+// curve", AIP Conf. Proc. 707 (2004): the grid coordinates are turned into the
+// curve's "transposed" index by reflections and exchanges from the top bit
+// down, Gray-decoded, and their bits interleaved (axis 0 most significant).  Consecutive indices are
 // face-adjacent cells, so a run of sorted bodies fills a compact region (the
 // Morton curve jumps between distant cells at every level boundary).
-__device__ __forceinline__ uint32_t hilbert_index30(uint32_t a0, uint32_t a1, uint32_t a2)
+__host__ __device__ __forceinline__ uint32_t hilbert_index30(uint32_t a0, uint32_t a1,
+                                                          uint32_t a2)
 {
     uint32_t X[3] = {a0, a1, a2};
     for (uint32_t q = 1u << 9; q > 1; q >>= 1) {
@@ -53,19 +55,40 @@ __device__ __forceinline__ uint32_t hilbert_index30(uint32_t a0, uint32_t a1, ui
     return (uint32_t)((spread21(X[0]) << 2) | (spread21(X[1]) << 1) | spread21(X[2]));
 }
 
+// The bits of a double as a 64-bit integer, and back.
+__host__ __device__ __forceinline__ long long bits_of(double v)
+{
+#ifdef __CUDA_ARCH__
+    return __double_as_longlong(v);
+#else
+    long long b;
+    memcpy(&b, &v, sizeof b);
+    return b;
+#endif
+}
+__host__ __device__ __forceinline__ double double_of(long long b)
+{
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double(b);
+#else
+    double v;
+    memcpy(&v, &b, sizeof v);
+    return v;
+#endif
+}
 // An FP64 value as a signed 64-bit key with the same order (negative values
 // have their magnitude bits flipped); the min/max reduction then runs on the
 // integer pipes (GB300's FP64 pipe is a small fraction of them).  NaN maps to
 // the neutral key, so it is ignored as fmin/fmax ignore it.
-__device__ __forceinline__ long long order_key(double v, long long nan_key)
+__host__ __device__ __forceinline__ long long order_key(double v, long long nan_key)
 {
-    const long long b = __double_as_longlong(v);
+    const long long b = bits_of(v);
     if ((b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll) return nan_key;
     return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
 }
-__device__ __forceinline__ double key_value(long long k)
+__host__ __device__ __forceinline__ double key_value(long long k)
 {
-    return __longlong_as_double(k >= 0 ? k : (k ^ 0x7fffffffffffffffll));
+    return double_of(k >= 0 ? k : (k ^ 0x7fffffffffffffffll));
 }
 
 } // namespace nb
