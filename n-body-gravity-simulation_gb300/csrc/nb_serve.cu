@@ -11,9 +11,9 @@
 //      - Barnes-Hut jobs each own a simulation object and run on one of
 //        kBHStreams streams (the process should allow that many hardware
 //        queues: CUDA_DEVICE_MAX_CONNECTIONS >= 16), each stream's jobs issued
-//        by its own host thread
-//        (a tree build reads its node count on the host, which then blocks
-//        only that stream's later jobs), overlapping with the direct batch and
+//        by that stream's thread of a pool kept for the server's lifetime (a
+//        tree build reads its node count on the host, which then blocks only
+//        that stream's later jobs), overlapping with the direct batch and
 //        with each other;
 //   3. retires jobs that reached their step count (state copied to the host,
 //      memory returned).
@@ -27,10 +27,13 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -121,6 +124,74 @@ double quantile(std::vector<double> v, double q)
     return v[lo] + (pos - (double)lo) * (v[hi] - v[lo]);
 }
 
+// One host thread per Barnes-Hut stream for the server's lifetime.  Each tick
+// dispatches a task to the busy streams (each thread issues its stream's
+// steps; a node-count read-back then blocks only that thread) and later waits
+// until all of them are done.
+class StreamPool {
+public:
+    void start(int threads, int device)
+    {
+        busy_.assign(threads, false);
+        for (int k = 0; k < threads; ++k) pool_.emplace_back([this, k, device] { loop(k, device); });
+    }
+    void dispatch(std::function<void(int)> task, const std::vector<bool> &busy)
+    {
+        std::lock_guard<std::mutex> lock(mu_);
+        task_ = std::move(task);
+        busy_ = busy;
+        pending_ = 0;
+        for (bool b : busy_) pending_ += b;
+        ++generation_;
+        cv_work_.notify_all();
+    }
+    void wait()
+    {
+        std::unique_lock<std::mutex> lock(mu_);
+        cv_done_.wait(lock, [this] { return pending_ == 0; });
+    }
+    void stop()
+    {
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            stop_ = true;
+            cv_work_.notify_all();
+        }
+        for (auto &t : pool_)
+            if (t.joinable()) t.join();
+        pool_.clear();
+    }
+
+private:
+    void loop(int k, int device)
+    {
+        cudaSetDevice(device);
+        uint64_t seen = 0;
+        while (true) {
+            std::function<void(int)> task;
+            {
+                std::unique_lock<std::mutex> lock(mu_);
+                cv_work_.wait(lock, [&] { return stop_ || generation_ != seen; });
+                if (stop_) return;
+                seen = generation_;
+                if (!busy_[k]) continue;
+                task = task_;
+            }
+            task(k);
+            std::lock_guard<std::mutex> lock(mu_);
+            if (--pending_ == 0) cv_done_.notify_all();
+        }
+    }
+    std::vector<std::thread> pool_;
+    std::mutex mu_;
+    std::condition_variable cv_work_, cv_done_;
+    std::function<void(int)> task_;
+    std::vector<bool> busy_;
+    uint64_t generation_ = 0;
+    int pending_ = 0;
+    bool stop_ = false;
+};
+
 } // namespace
 } // namespace nb
 
@@ -128,6 +199,7 @@ struct nb_server {
     nb_server_config cfg{};
     cudaStream_t stream = nullptr;
     cudaStream_t bh_streams[nb::kBHStreams] = {};
+    nb::StreamPool pool_threads;  // issues the Barnes-Hut streams' steps
     size_t ps = 0;
     nb::DevBuf pool, hi, lo, d_sys, d_items, d_counter, d_new_sys, d_new_items;
     double *f[10] = {};
@@ -345,20 +417,11 @@ nb_status tick(nb_server *s)
     // BH streams wait for the tick start so that latencies share one origin
     for (int k = 0; k < kBHStreams; ++k)
         NB_CUDA_TRY(cudaStreamWaitEvent(s->bh_streams[k], s->tick_start, 0));
-    // Barnes-Hut jobs: one host thread per busy stream; this thread issues the
-    // direct batch meanwhile
+    // Barnes-Hut jobs: the pool's thread of each busy stream issues that
+    // stream's steps; this thread issues the direct batch meanwhile
     std::vector<std::vector<Job *>> per_stream(kBHStreams);
     for (Job *j : bh) per_stream[j->stream_index].push_back(j);
-    std::vector<nb_status> bh_status(kBHStreams, NB_OK);
-    std::vector<std::string> bh_error(kBHStreams);
-    int device = 0;
-    NB_CUDA_TRY(cudaGetDevice(&device));
     auto run_stream = [&](int k) {
-        if (cudaSetDevice(device) != cudaSuccess) {
-            bh_status[k] = NB_ERR_CUDA;
-            bh_error[k] = "cudaSetDevice failed in a Barnes-Hut stream thread";
-            return;
-        }
         for (Job *j : per_stream[k]) {
             nb_status r = nb_step(j->sim, NB_LEAPFROG, dt, 1);
             if (r == NB_OK) {
@@ -371,17 +434,14 @@ nb_status tick(nb_server *s)
             }
         }
     };
-    std::vector<std::thread> workers;
-    for (int k = 0; k < kBHStreams; ++k)
-        if (!per_stream[k].empty()) workers.emplace_back(run_stream, k);
-    struct Joiner {
-        std::vector<std::thread> &w;
-        ~Joiner()
-        {
-            for (auto &t : w)
-                if (t.joinable()) t.join();
-        }
-    } joiner{workers};
+    std::vector<bool> busy(kBHStreams);
+    for (int k = 0; k < kBHStreams; ++k) busy[k] = !per_stream[k].empty();
+    s->pool_threads.dispatch(run_stream, busy);
+    // wait for the stream threads even when the direct batch below fails
+    struct Waiter {
+        StreamPool &p;
+        ~Waiter() { p.wait(); }
+    } waiter{s->pool_threads};
     const auto t_direct = Clock::now();
     if (!direct.empty()) {
         float4 *hi = s->hi.as<float4>(), *lo = s->lo.as<float4>();
@@ -407,10 +467,8 @@ nb_status tick(nb_server *s)
     }
     s->direct_ms += ms_since(t_direct);
     const auto t_join = Clock::now();
-    for (auto &t : workers) t.join();
+    s->pool_threads.wait();
     s->join_ms += ms_since(t_join);
-    for (int k = 0; k < kBHStreams; ++k)
-        if (bh_status[k] != NB_OK) return fail(bh_status[k], bh_error[k]);
     s->issue_ms += ms_since(t_phase);
     t_phase = Clock::now();
     NB_CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -496,6 +554,9 @@ nb_status nb_server_create(const nb_server_config *cfg, nb_server **out)
     }
     for (int k = 0; k < 10; ++k) s->f[k] = s->pool.as<double>() + k * s->ps;
     s->slots.init(cfg->pool_bodies);
+    int device = 0;
+    cudaGetDevice(&device);
+    s->pool_threads.start(kBHStreams, device);
     s->peak_bytes = pool_bytes(s);
     *out = s;
     return NB_OK;
@@ -504,6 +565,7 @@ nb_status nb_server_create(const nb_server_config *cfg, nb_server **out)
 nb_status nb_server_destroy(nb_server *s)
 {
     if (!s) return NB_OK;
+    s->pool_threads.stop();
     if (s->stream) cudaStreamSynchronize(s->stream);
     for (auto &j : s->running) {
         if (j->sim) nb_destroy(j->sim);
