@@ -138,13 +138,13 @@ batch_force_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
 
 int batch_grid()
 {
-    static int grid = 0;
-    if (!grid) {
+    // a function-local static: initialised once, thread-safe
+    static const int grid = [] {
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &per_sm, (const void *)batch_force_kernel<false>, kBatchBlock, 0);
-        grid = std::max(1, per_sm) * device_props().num_sms;
-    }
+        return std::max(1, per_sm) * device_props().num_sms;
+    }();
     return grid;
 }
 
@@ -466,13 +466,12 @@ batch_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo
 
 int batch_sorted_grid()
 {
-    static int grid = 0;
-    if (!grid) {
+    static const int grid = [] {
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &per_sm, (const void *)batch_sorted_kernel<false>, kBatchBlock, 0);
-        grid = std::max(1, per_sm) * device_props().num_sms;
-    }
+        return std::max(1, per_sm) * device_props().num_sms;
+    }();
     return grid;
 }
 

@@ -287,8 +287,7 @@ constexpr int kNumMixShapes = sizeof(kMixShapes) / sizeof(kMixShapes[0]);
 template <int B, int I>
 int mix_slots()
 {
-    static int slots = 0;
-    if (!slots) slots = resident_ctas<B, I>((const void *)direct_mixed_kernel<B, I, false>);
+    static const int slots = resident_ctas<B, I>((const void *)direct_mixed_kernel<B, I, false>);
     return slots;
 }
 
@@ -481,8 +480,7 @@ static nb_status direct_fp64_shape(const double *x, const double *y, const doubl
     const int per_cta = B * I;
     const int iblocks = (n + per_cta - 1) / per_cta;
     const int tiles = (n + B - 1) / B;
-    static int slots = 0;
-    if (!slots) slots = resident_ctas<B, I>((const void *)direct_fp64_kernel<B, I, false>);
+    static const int slots = resident_ctas<B, I>((const void *)direct_fp64_kernel<B, I, false>);
     int segs = pick_segments(iblocks, tiles, slots);
     const int seg_tiles = (tiles + segs - 1) / segs;
     segs = (tiles + seg_tiles - 1) / seg_tiles;

@@ -301,13 +301,12 @@ constexpr int kNumSortedShapes = sizeof(kSortedShapes) / sizeof(kSortedShapes[0]
 template <int W, int I>
 int sorted_slots()
 {
-    static int slots = 0;
-    if (!slots) {
+    static const int slots = [] {
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &per_sm, (const void *)direct_sorted_kernel<W, I, false>, W * 32, 0);
-        slots = std::max(1, per_sm) * device_props().num_sms;
-    }
+        return std::max(1, per_sm) * device_props().num_sms;
+    }();
     return slots;
 }
 
