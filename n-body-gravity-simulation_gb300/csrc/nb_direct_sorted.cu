@@ -423,8 +423,14 @@ static nb_status run_sorted(const DirectPlan &p, const float4 *hi, const float4 
     return NB_OK;
 }
 
+// Times every CTA shape, each with the modelled j-split and with 1.5 times as
+// many segments (shorter CTAs balance better at the end of the launch but
+// give the combine more partials to read), kernel and combine together (the
+// combine writes the real outputs, which the evaluation then overwrites), and
+// records the fastest plan for this n.
 static nb_status autotune_sorted(const float4 *hi, const float4 *lo, int n, double eps2,
-                                 SortedBuffers &b, cudaStream_t st, DirectPlan *best)
+                                 double G, const uint32_t *order, double *ax, double *ay,
+                                 double *az, SortedBuffers &b, cudaStream_t st, DirectPlan *best)
 {
     cudaEvent_t e0, e1;
     NB_CUDA_TRY(cudaEventCreate(&e0));
@@ -433,24 +439,43 @@ static nb_status autotune_sorted(const float4 *hi, const float4 *lo, int n, doub
     // Above 2^18 bodies every shape is timed on all i-bodies against the first
     // 512 j-chunks only (one segment): an evaluation there takes 0.1 s and more.
     const bool probe = n > (1 << 18);
+    const int nchunks = (n + kChunk - 1) / kChunk;
     for (int k = 0; k < kNumSortedShapes; ++k) {
-        const DirectPlan p = sorted_plan_for_shape(n, kSortedShapes[k].warps, kSortedShapes[k].ipt);
-        DirectPlan t = p;
-        if (probe) {
-            t.segments = 1;
-            t.seg_tiles = std::min(p.seg_tiles * p.segments, 512);
+        const DirectPlan p0 = sorted_plan_for_shape(n, kSortedShapes[k].warps, kSortedShapes[k].ipt);
+        DirectPlan variants[2] = {p0, p0};
+        int num_variants = 1;
+        if (!probe) {
+            const int s1 = (3 * p0.segments + 1) / 2;
+            DirectPlan &v = variants[1];
+            v.seg_tiles = std::max(1, (nchunks + s1 - 1) / s1);
+            v.segments = (nchunks + v.seg_tiles - 1) / v.seg_tiles;
+            if (v.segments != p0.segments) num_variants = 2;
         }
-        float *psum = nullptr;
-        NB_TRY(run_sorted(t, hi, lo, n, eps2, b, st, &psum));
-        cudaEventRecord(e0, st);
-        for (int r = 0; r < 2; ++r) NB_TRY(run_sorted(t, hi, lo, n, eps2, b, st, &psum));
-        cudaEventRecord(e1, st);
-        NB_CUDA_TRY(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best_ms) {
-            best_ms = ms;
-            *best = p;
+        for (int vi = 0; vi < num_variants; ++vi) {
+            const DirectPlan &p = variants[vi];
+            DirectPlan t = p;
+            if (probe) {
+                t.segments = 1;
+                t.seg_tiles = std::min(p.seg_tiles * p.segments, 512);
+            }
+            float *psum = nullptr;
+            NB_TRY(run_sorted(t, hi, lo, n, eps2, b, st, &psum));
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < 2; ++r) {
+                NB_TRY(run_sorted(t, hi, lo, n, eps2, b, st, &psum));
+                combine_sorted_kernel<<<(n + 255) / 256, 256, 0, st>>>(
+                    psum, psum + 3 * (size_t)n * t.segments, n, t.segments, G, order, ax, ay,
+                    az);
+                NB_LAUNCH_CHECK();
+            }
+            cudaEventRecord(e1, st);
+            NB_CUDA_TRY(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best_ms) {
+                best_ms = ms;
+                *best = p;
+            }
         }
     }
     cudaEventDestroy(e0);
@@ -498,7 +523,8 @@ nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
     }
     if (!tuned) {
         const char *e = std::getenv("NB_AUTOTUNE");
-        if (!(e && std::strcmp(e, "0") == 0)) NB_TRY(autotune_sorted(hi, lo, n, eps2, b, st, &p));
+        if (!(e && std::strcmp(e, "0") == 0))
+            NB_TRY(autotune_sorted(hi, lo, n, eps2, G, order, ax, ay, az, b, st, &p));
         else p = sorted_plan_for_shape(n, 4, 4);
     }
     if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
