@@ -11,6 +11,8 @@ import pytest
 
 from conftest import REPO
 
+HEADER = os.path.join(REPO, "include", "nbody_c.h")
+
 
 def declared_functions():
     names = set()
@@ -45,6 +47,13 @@ def test_status_strings_and_version(nb):
     L = nb.lib()
     assert L.nb_status_string(0) == b"ok"
     assert L.nb_status_string(4) == b"capacity exceeded"
+    assert L.nb_status_string(9) == b"cancelled"
+    # every status the header declares has its own string and a Python name
+    codes = [int(c) for c in re.findall(r"NB_(?:OK|ERR_[A-Z_]+) = (\d+)", open(HEADER).read())]
+    assert sorted(codes) == list(range(len(codes)))
+    assert set(codes) == set(nb.STATUS)
+    names = {L.nb_status_string(c) for c in codes}
+    assert len(names) == len(codes) and b"unknown status" not in names
     assert b"sm_103a" in L.nb_version()
 
 
