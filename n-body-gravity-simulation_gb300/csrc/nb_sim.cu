@@ -425,8 +425,15 @@ static nb_status load_impl(nb_sim *s, size_t n, const double *const *src, cudaMe
     const size_t bytes = n * sizeof(double);
     for (int k = 0; k < 7 && n > 0; ++k)
         NB_CUDA_TRY(cudaMemcpyAsync(s->f[dst_plane[k]], src[k], bytes, kind, s->stream));
-    for (int k = 6; k < 9 && n > 0; ++k)
-        NB_CUDA_TRY(cudaMemsetAsync(s->f[k], 0, bytes, s->stream));
+    // a = 0 until forces are computed: one memset when the three planes are
+    // the engine's own (adjacent in its state allocation), else one per plane
+    const size_t ps = plane_stride(s->capacity);
+    const double *own = s->state.as<double>();
+    if (n > 0 && s->f[6] == own + 6 * ps && s->f[7] == own + 7 * ps && s->f[8] == own + 8 * ps)
+        NB_CUDA_TRY(cudaMemsetAsync(s->f[6], 0, sizeof(double) * (2 * ps + n), s->stream));
+    else
+        for (int k = 6; k < 9 && n > 0; ++k)
+            NB_CUDA_TRY(cudaMemsetAsync(s->f[k], 0, bytes, s->stream));
     s->n = n;
     s->forces_valid = false;
     bh_invalidate(s->bh);
