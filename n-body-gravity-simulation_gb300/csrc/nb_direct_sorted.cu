@@ -63,46 +63,49 @@ constexpr int kResortEvals = 8;        // force evaluations per re-sort
 constexpr bool kHilbertOrder = true;   // sort along the Hilbert curve (else Morton)
 
 // Positions in sorted order relative to the root centre, split into
-// double-single hi/lo parts; mass in hi.w.
+// double-single hi/lo parts (mass in hi.w), and the bounding box of the hi
+// positions of every 32-body chunk (a warp is a chunk: box[2t] = min,
+// box[2t+1] = max; lanes past n take the chunk's first body).  Blocks are
+// multiples of 32 threads.
 __global__ void split_sorted_kernel(const uint32_t *__restrict__ order,
                                     const double *__restrict__ x, const double *__restrict__ y,
                                     const double *__restrict__ z, const double *__restrict__ m,
                                     int n, const double *__restrict__ centre,
-                                    float4 *__restrict__ hi, float4 *__restrict__ lo)
+                                    float4 *__restrict__ hi, float4 *__restrict__ lo,
+                                    float4 *__restrict__ box)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t o = order[i];
-    if (!NB_IN_RANGE(o, n)) return;
-    const double X = x[o] - centre[0], Y = y[o] - centre[1], Z = z[o] - centre[2];
-    const float hx = __double2float_rn(X), hy = __double2float_rn(Y), hz = __double2float_rn(Z);
-    hi[i] = make_float4(hx, hy, hz, __double2float_rn(m[o]));
-    lo[i] = make_float4(__double2float_rn(X - (double)hx), __double2float_rn(Y - (double)hy),
-                        __double2float_rn(Z - (double)hz), 0.0f);
-}
-
-// Bounding box of every chunk of 32 consecutive sorted bodies (one warp per
-// chunk): box[2t] = min, box[2t+1] = max.  Lanes past n repeat the chunk's
-// first body, which is valid.
-__global__ void chunk_box_kernel(const float4 *__restrict__ hi, int n, int nchunks,
-                                 float4 *__restrict__ box)
-{
-    const int t = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-    const int lane = threadIdx.x & 31;
-    if (t >= nchunks) return;
-    const int i = t * kChunk + lane;
-    const float4 p = hi[i < n ? i : t * kChunk];
-    float mn[3] = {p.x, p.y, p.z}, mx[3] = {p.x, p.y, p.z};
+    const int chunk = i / kChunk, lane = threadIdx.x & 31;
+    if (chunk * kChunk >= n) return;  // the whole warp is past n
+    float p[3] = {0.f, 0.f, 0.f};
+    const uint32_t o = i < n ? order[i] : 0u;
+    if (i < n && NB_IN_RANGE(o, n)) {
+        const double X = x[o] - centre[0], Y = y[o] - centre[1], Z = z[o] - centre[2];
+        const float hx = __double2float_rn(X), hy = __double2float_rn(Y),
+                    hz = __double2float_rn(Z);
+        hi[i] = make_float4(hx, hy, hz, __double2float_rn(m[o]));
+        lo[i] = make_float4(__double2float_rn(X - (double)hx), __double2float_rn(Y - (double)hy),
+                            __double2float_rn(Z - (double)hz), 0.0f);
+        p[0] = hx;
+        p[1] = hy;
+        p[2] = hz;
+    }
+    float mn[3], mx[3];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
+    for (int k = 0; k < 3; ++k) {
+        const float first = __shfl_sync(0xffffffffu, p[k], 0);
+        mn[k] = mx[k] = i < n ? p[k] : first;
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1)
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
-            mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+            mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], s));
+            mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], s));
         }
     if (lane == 0) {
-        box[2 * t] = make_float4(mn[0], mn[1], mn[2], 0.f);
-        box[2 * t + 1] = make_float4(mx[0], mx[1], mx[2], 0.f);
+        box[2 * chunk] = make_float4(mn[0], mn[1], mn[2], 0.f);
+        box[2 * chunk + 1] = make_float4(mx[0], mx[1], mx[2], 0.f);
     }
 }
 
@@ -509,9 +512,8 @@ nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
     NB_TRY(b.lo.reserve(sizeof(float4) * (size_t)n));
     NB_TRY(b.boxes.reserve(sizeof(float4) * 2 * (size_t)nchunks));
     float4 *hi = b.hi.as<float4>(), *lo = b.lo.as<float4>();
-    split_sorted_kernel<<<(n + 255) / 256, 256, 0, st>>>(order, x, y, z, m, n, centre, hi, lo);
-    NB_LAUNCH_CHECK();
-    chunk_box_kernel<<<(nchunks + 7) / 8, 256, 0, st>>>(hi, n, nchunks, b.boxes.as<float4>());
+    split_sorted_kernel<<<(n + 255) / 256, 256, 0, st>>>(order, x, y, z, m, n, centre, hi, lo,
+                                                         b.boxes.as<float4>());
     NB_LAUNCH_CHECK();
     DirectPlan p;
     bool tuned;
