@@ -41,7 +41,7 @@ mv -f "$HERE/_ref/libnbref.so.tmp" "$HERE/_ref/libnbref.so"
 # CUDA/src/force_calculator_naive.cu:4-59) as a standalone sm_103a cubin, compiled
 # where it lies with the reference Makefile's flags (-std=c++17 -O3) and the
 # architecture switched to sm_103a.  Device code only: it carries no host code,
-# so it runs on any host of the GPU machine; ref_gpu.py loads it with the driver API.
+# so it runs on any sm_103a host (x86 or Arm); ref_gpu.py loads it with the CUDA driver API.
 CUDA_SRC="$REF_ROOT/CUDA/src/force_calculator_naive.cu"
 NVCC="${NVCC:-$(command -v nvcc || echo /usr/local/cuda/bin/nvcc)}"
 if [[ -f "$CUDA_SRC" && -x "$NVCC" ]]; then

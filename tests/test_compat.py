@@ -77,7 +77,7 @@ def test_compat_forces_driver(nb, oracle, tmp_path):
     x, y, z, m = (raw[1 + k * n:1 + (k + 1) * n] for k in range(4))
     a_naive = raw[1 + 4 * n:1 + 7 * n].reshape(3, n)
     a_bh = raw[1 + 7 * n:1 + 10 * n].reshape(3, n)
-    # the driver's std::mt19937 draws are the CUDA benchmark's order; the host
+    # the test program's std::mt19937 draws are the CUDA benchmark's order; the host
     # compiler may fuse libstdc++'s u*(b-a)+a into an FMA (Arm), so allow an ulp
     g = oracle.MT19937(42)
     ox, oy, oz, om = g.uniform_cube(n, order=1)
