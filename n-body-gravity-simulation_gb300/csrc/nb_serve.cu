@@ -130,10 +130,18 @@ double quantile(std::vector<double> v, double q)
 // until all of them are done.
 class StreamPool {
 public:
-    void start(int threads, int device)
+    // false when the threads cannot be created (the pool is then empty)
+    bool start(int threads, int device)
     {
         busy_.assign(threads, false);
-        for (int k = 0; k < threads; ++k) pool_.emplace_back([this, k, device] { loop(k, device); });
+        try {
+            for (int k = 0; k < threads; ++k)
+                pool_.emplace_back([this, k, device] { loop(k, device); });
+        } catch (...) {
+            stop();
+            return false;
+        }
+        return true;
     }
     void dispatch(std::function<void(int)> task, const std::vector<bool> &busy)
     {
@@ -556,7 +564,10 @@ nb_status nb_server_create(const nb_server_config *cfg, nb_server **out)
     s->slots.init(cfg->pool_bodies);
     int device = 0;
     cudaGetDevice(&device);
-    s->pool_threads.start(kBHStreams, device);
+    if (!s->pool_threads.start(kBHStreams, device)) {
+        nb_server_destroy(s);
+        return fail(NB_ERR_CUDA, "server: cannot start the Barnes-Hut stream threads");
+    }
     s->peak_bytes = pool_bytes(s);
     *out = s;
     return NB_OK;
