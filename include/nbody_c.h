@@ -104,7 +104,11 @@ typedef struct nb_config {
 /* NB_DIRECT_MIXED kernel choice.  By default systems of at least 16,384 bodies
  * take the Hilbert-sorted near/far kernel (far j-chunks in plain FP32 relative to
  * a warp-local origin) and smaller ones the all-pairs double-single kernel;
- * these flags force one or the other (same accuracy criteria either way). */
+ * these flags force one or the other (same accuracy criteria either way).
+ * Both kernels time their tile shapes and j-splits on the first evaluation of
+ * each N in a process and keep the fastest; results are bit-identical within a
+ * process, and between processes when the environment sets NB_AUTOTUNE=0
+ * (fixed shapes), since the j-split decides the summation order. */
 #define NB_FLAG_MIXED_SORTED 4
 #define NB_FLAG_MIXED_UNSORTED 8
 
