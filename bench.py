@@ -184,15 +184,21 @@ def fp32_roofline_gint(num_sms: int, mhz: float) -> float:
     return num_sms * mhz * 1e6 * 128.0 / 12.0 / 1e9
 
 
-def cpu_reference_rate(n, target_seconds, threads=0):
-    """The reference's FP64 direct sum on the host cores (its C restatement),
-    timed on a bounded sample of i-rows of the same workload."""
+def load_oracle():
     sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import nbody_gb300 as nb
     import oracle as O
     if not os.path.exists(O.LIB_PATH):
         O.build(with_ref=False)
-    x, y, z, vx, vy, vz, m = nb.plummer(n, seed=SEED)
+    return O
+
+
+def cpu_reference_rate(n, target_seconds, threads=0):
+    """The reference's FP64 direct sum on the host cores (its C restatement),
+    timed on a bounded sample of i-rows of the same workload.  The inputs come
+    from the oracle's restatement of the engine's generator (the same bits), so
+    this process never loads the engine library."""
+    O = load_oracle()
+    x, y, z, vx, vy, vz, m = O.plummer(n, seed=SEED)
     cores = O.threads() if threads == 0 else threads
     rows = 256
     t0 = time.perf_counter()

@@ -431,16 +431,24 @@ nb_status nb_checkpoint_load(nb_sim *sim, const char *path);
  * that may not allocate device memory (a host whose device memory is owned by
  * its own pool allocator, a plugin with a fixed device-memory budget, a loop
  * that cannot take the implicit synchronisation of cudaMalloc/cudaFree).
- * Computes G-scaled accelerations of n bodies exactly as the NB_DIRECT_MIXED
- * method does, from caller-owned DEVICE arrays x, y, z, m into caller-owned
- * DEVICE arrays ax, ay, az, on `stream` (NULL = legacy default stream),
- * asynchronously.  It allocates nothing: its scratch is one 16 MiB array in
- * the library's device memory, present on every device that loads the
- * library until the process exits, which limits n to 262144 (larger n returns
+ * Computes G-scaled accelerations of n bodies with the all-pairs mixed kernels
+ * (split, all-pairs sum, combine) from caller-owned DEVICE arrays x, y, z, m
+ * into caller-owned DEVICE arrays ax, ay, az, on `stream` (NULL = legacy
+ * default stream), asynchronously.  It never runs the Hilbert-sorted kernel
+ * that NB_DIRECT_MIXED uses from 16,384 bodies, never autotunes, and caps its
+ * j-split to fit its scratch, so it agrees with NB_DIRECT_MIXED to the
+ * mixed-path tolerance; its bits equal those of an NB_DIRECT_MIXED evaluation
+ * only when both run the same plan (the all-pairs kernel with autotuning off,
+ * NB_AUTOTUNE=0, and n small enough that the j-split is not capped, about
+ * n < 150,000).  It allocates nothing: its scratch is one 16 MiB array in the
+ * library's device memory, present on every device that loads the library
+ * until the process exits, which limits n to 262144 (larger n returns
  * NB_ERR_CAPACITY).  The first call on each device looks up that array's
  * device address (cudaGetSymbolAddress) and must run with that device current
- * and before any stream capture.  All calls share the array: calls whose work
- * overlaps on the GPU race and must be serialised by the caller. */
+ * and before any stream capture; the address is kept for the life of the
+ * process, so the entry point must not be used on a device after
+ * cudaDeviceReset.  All calls share the array: calls whose work overlaps on
+ * the GPU race and must be serialised by the caller. */
 nb_status nb_direct_mixed_forces_noalloc(size_t n, const double *x, const double *y,
                                          const double *z, const double *m, double G,
                                          double softening, double *ax, double *ay, double *az,

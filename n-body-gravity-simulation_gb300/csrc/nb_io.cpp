@@ -70,7 +70,10 @@ nb_status parse_particles(const char *path, size_t capacity, size_t *n, double *
     if (!read_all(path, text)) return fail(NB_ERR_IO, io_msg("cannot read particle file", path));
     Tokens tk{text.data(), text.data() + text.size()};
     double count = 0.0;
-    if (!tk.next_double(count) || count < 0.0 || count != (double)(long long)count)
+    // the range test comes first: converting a double beyond long long's
+    // range is undefined, and no file holds 2^53 bodies
+    if (!tk.next_double(count) || !(count >= 0.0 && count <= 9.0e15) ||
+        count != (double)(long long)count)
         return fail(NB_ERR_IO, std::string("particle file '") + path +
                                    "': the first token is not a body count");
     const size_t N = (size_t)count;

@@ -36,6 +36,8 @@ REF_SOURCES=(
     -I"$REF_ROOT/CPU/include" -o "$HERE/_ref/libnbref.so.tmp" \
     "$HERE/ref_shim.cpp" "${REF_SOURCES[@]}"
 mv -f "$HERE/_ref/libnbref.so.tmp" "$HERE/_ref/libnbref.so"
+# where the reference lies, for the tests that read its fixtures and programs
+printf '%s\n' "$REF_ROOT" > "$HERE/_ref/ref_root.txt"
 
 # The reference's FP64 GPU kernel (computeAccelerationNaiveKernel,
 # CUDA/src/force_calculator_naive.cu:4-59) as a standalone sm_103a cubin, compiled

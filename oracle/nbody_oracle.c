@@ -1157,3 +1157,164 @@ ORC_API int orc_octree(int n, const uint64_t *sc, int leaf_capacity, int levels,
     }
     return nn;
 }
+
+/* ------------------------------------------------------------------------
+ * 8. Synthetic workload generators.
+ *
+ * The benchmark configurations (Plummer spheres, the disk + bulge system)
+ * have no reference code.  This section restates the engine's own seeded
+ * generators (n-body-gravity-simulation_gb300/csrc/nb_gen.cpp) in C so that
+ * the CPU arms of the benchmark can build their inputs without loading the
+ * engine library; a test checks that both give the same bits.
+ *   - SplitMix64 (Steele, Lea & Flood 2014), one stream per body keyed by
+ *     (seed, body index); uniform draws on (0, 1) from the top 53 bits.
+ *   - Plummer: Aarseth, Henon & Wielen (1974): radius from the cumulative
+ *     mass truncated at 99.9 %, speed by von Neumann rejection on
+ *     q^2 (1 - q^2)^(7/2) in units of the local escape speed.
+ *   - Exponential disk: radius by inverting 1 - (1 + y) e^-y = u
+ *     (bracketed Newton), sech^2 vertical profile, circular speed of the
+ *     enclosed bulge + disk mass with a Gaussian dispersion.
+ * All arithmetic is FP64 with the same operation order as the engine's. */
+#define ORC_PI 3.14159265358979323846
+
+typedef struct {
+    uint64_t s;
+} orc_sm64;
+
+static uint64_t orc_sm64_next(orc_sm64 *r)
+{
+    uint64_t z = (r->s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static void orc_sm64_init(orc_sm64 *r, uint64_t seed, uint64_t body)
+{
+    r->s = seed * 0xD1B54A32D192ED03ull ^ (body + 1) * 0x9E3779B97F4A7C15ull;
+    (void)orc_sm64_next(r);
+}
+
+static double orc_sm64_u(orc_sm64 *r)
+{
+    return ((double)(orc_sm64_next(r) >> 11) + 0.5) * 0x1.0p-53;
+}
+
+static double orc_sm64_normal(orc_sm64 *r)
+{
+    const double a = orc_sm64_u(r), b = orc_sm64_u(r);
+    return sqrt(-2.0 * log(a)) * cos(2.0 * ORC_PI * b);
+}
+
+static void orc_isotropic(orc_sm64 *r, double len, double *x, double *y, double *z)
+{
+    const double c = 1.0 - 2.0 * orc_sm64_u(r);
+    const double one_c2 = 1.0 - c * c;
+    const double s = sqrt(one_c2 > 0.0 ? one_c2 : 0.0);
+    const double phi = 2.0 * ORC_PI * orc_sm64_u(r);
+    *x = len * s * cos(phi);
+    *y = len * s * sin(phi);
+    *z = len * c;
+}
+
+static void orc_plummer_body(orc_sm64 *r, double M, double a, double G, double *p, double *v)
+{
+    const double X1 = 0.999 * orc_sm64_u(r);
+    const double rad = a / sqrt(pow(X1, -2.0 / 3.0) - 1.0);
+    orc_isotropic(r, rad, &p[0], &p[1], &p[2]);
+    double q = 0.0;
+    for (int it = 0; it < 100000; ++it) {
+        q = orc_sm64_u(r);
+        const double g = 0.1 * orc_sm64_u(r);
+        if (g < q * q * pow(1.0 - q * q, 3.5)) break;
+    }
+    const double ve = sqrt(2.0 * G * M / a) * pow(1.0 + rad * rad / (a * a), -0.25);
+    orc_isotropic(r, q * ve, &v[0], &v[1], &v[2]);
+}
+
+static void orc_to_com_frame(int n, const double *m, double *x, double *y, double *z,
+                             double *vx, double *vy, double *vz)
+{
+    double M = 0, c[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < n; ++i) {
+        M += m[i];
+        c[0] += m[i] * x[i]; c[1] += m[i] * y[i]; c[2] += m[i] * z[i];
+        c[3] += m[i] * vx[i]; c[4] += m[i] * vy[i]; c[5] += m[i] * vz[i];
+    }
+    if (!(M > 0)) return;
+    for (int k = 0; k < 6; ++k) c[k] /= M;
+    for (int i = 0; i < n; ++i) {
+        x[i] -= c[0]; y[i] -= c[1]; z[i] -= c[2];
+        vx[i] -= c[3]; vy[i] -= c[4]; vz[i] -= c[5];
+    }
+}
+
+static double orc_disk_radius(double u)
+{
+    double lo = 0.0, hi = 50.0, y = 1.0;
+    for (int it = 0; it < 200; ++it) {
+        const double f = 1.0 - (1.0 + y) * exp(-y) - u;
+        if (f > 0) hi = y; else lo = y;
+        const double df = y * exp(-y);
+        double yn = (df > 0) ? y - f / df : 0.5 * (lo + hi);
+        if (!(yn > lo && yn < hi)) yn = 0.5 * (lo + hi);
+        if (fabs(yn - y) < 1e-15 * (1.0 + y)) { y = yn; break; }
+        y = yn;
+    }
+    return y;
+}
+
+ORC_API void orc_gen_plummer(int n, uint64_t seed, double total_mass, double scale, double G,
+                             double *x, double *y, double *z, double *vx, double *vy, double *vz,
+                             double *m)
+{
+    for (int i = 0; i < n; ++i) {
+        orc_sm64 r;
+        orc_sm64_init(&r, seed, (uint64_t)i);
+        double p[3], v[3];
+        orc_plummer_body(&r, total_mass, scale, G, p, v);
+        x[i] = p[0]; y[i] = p[1]; z[i] = p[2];
+        vx[i] = v[0]; vy[i] = v[1]; vz[i] = v[2];
+        m[i] = total_mass / (double)n;
+    }
+    orc_to_com_frame(n, m, x, y, z, vx, vy, vz);
+}
+
+ORC_API void orc_gen_disk_bulge(int n, uint64_t seed, double total_mass, double bulge_frac,
+                                double bulge_scale, double disk_scale, double disk_height,
+                                double dispersion, double G, double *x, double *y, double *z,
+                                double *vx, double *vy, double *vz, double *m)
+{
+    const int nbulge = (int)llround(bulge_frac * (double)n);
+    const double Mb = total_mass * bulge_frac, Md = total_mass - Mb;
+    for (int i = 0; i < n; ++i) {
+        orc_sm64 r;
+        orc_sm64_init(&r, seed, (uint64_t)i);
+        m[i] = total_mass / (double)n;
+        double p[3], v[3];
+        if (i < nbulge) {
+            orc_plummer_body(&r, Mb, bulge_scale, G, p, v);
+        } else {
+            const double R = disk_scale * orc_disk_radius(0.999 * orc_sm64_u(&r));
+            const double phi = 2.0 * ORC_PI * orc_sm64_u(&r);
+            double uz = orc_sm64_u(&r);
+            uz = uz < 5e-4 ? 5e-4 : uz;
+            uz = uz > 1.0 - 5e-4 ? 1.0 - 5e-4 : uz;
+            p[0] = R * cos(phi);
+            p[1] = R * sin(phi);
+            p[2] = disk_height * atanh(2.0 * uz - 1.0);
+            const double rs = sqrt(R * R + p[2] * p[2]);
+            const double yd = R / disk_scale;
+            const double menc = Mb * rs * rs * rs / pow(rs * rs + bulge_scale * bulge_scale, 1.5) +
+                                Md * (1.0 - (1.0 + yd) * exp(-yd));
+            const double vc = (R > 0) ? sqrt(G * menc / (rs > 1e-12 ? rs : 1e-12)) : 0.0;
+            const double sig = dispersion * vc;
+            v[0] = -vc * sin(phi) + sig * orc_sm64_normal(&r);
+            v[1] = vc * cos(phi) + sig * orc_sm64_normal(&r);
+            v[2] = sig * orc_sm64_normal(&r);
+        }
+        x[i] = p[0]; y[i] = p[1]; z[i] = p[2];
+        vx[i] = v[0]; vy[i] = v[1]; vz[i] = v[2];
+    }
+    orc_to_com_frame(n, m, x, y, z, vx, vy, vz);
+}

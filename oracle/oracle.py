@@ -84,6 +84,11 @@ def lib():
                                  _i32p, _i32p, _i32p, _i32p, _i32p]
         L.orc_octree.restype = C.c_int
         L.orc_max_threads.restype = C.c_int
+        L.orc_gen_plummer.argtypes = [C.c_int, C.c_uint64, C.c_double, C.c_double, C.c_double,
+                                      _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.orc_gen_disk_bulge.argtypes = [C.c_int, C.c_uint64, C.c_double, C.c_double,
+                                         C.c_double, C.c_double, C.c_double, C.c_double,
+                                         C.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -284,3 +289,21 @@ def error_stats(a_test, a_ref):
     rel = np.where(mask, d / np.where(mask, r, 1.0), 0.0)
     return dict(avg_abs=float(d.sum() / n), max_abs=float(d.max(initial=0.0)),
                 avg_rel=float(rel.sum() / n), max_rel=float(rel.max(initial=0.0)))
+
+
+def plummer(n, seed=0, total_mass=1.0, scale=1.0, G=1.0):
+    """The engine's seeded Plummer sphere, restated (section 8 of the C file):
+    (x, y, z, vx, vy, vz, m) as float64 arrays, the same bits as the engine's
+    generator."""
+    out = [np.empty(n) for _ in range(7)]
+    lib().orc_gen_plummer(n, seed, total_mass, scale, G, *out)
+    return tuple(out)
+
+
+def disk_bulge(n, seed=0, total_mass=1.0, bulge_frac=0.2, bulge_scale=0.2, disk_scale=1.0,
+               disk_height=0.05, dispersion=0.1, G=1.0):
+    """The engine's seeded Plummer bulge + exponential disk, restated."""
+    out = [np.empty(n) for _ in range(7)]
+    lib().orc_gen_disk_bulge(n, seed, total_mass, bulge_frac, bulge_scale, disk_scale,
+                             disk_height, dispersion, G, *out)
+    return tuple(out)

@@ -13,6 +13,20 @@ for p in (REPO, PKG_DIR, ORACLE_DIR):
         sys.path.insert(0, p)
 
 
+def ref_root():
+    """Where the reference checkout lies, or None: $REF_ROOT, else the location
+    oracle/build_ref.sh recorded when it compiled the reference here
+    (oracle/_ref/ref_root.txt).  Tests that read reference files skip without it."""
+    env = os.environ.get("REF_ROOT")
+    if env:
+        return env if os.path.isdir(env) else None
+    rec = os.path.join(ORACLE_DIR, "_ref", "ref_root.txt")
+    if os.path.exists(rec):
+        path = open(rec).read().strip()
+        return path if os.path.isdir(path) else None
+    return None
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (run with -m gpu)")
 

@@ -15,9 +15,9 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import PKG_DIR, REPO
+from conftest import PKG_DIR, REPO, ref_root
 
-REF = os.environ.get("REF_ROOT", "/root/reference")
+REF = ref_root() or ""
 COMPAT_INC = os.path.join(PKG_DIR, "compat", "include")
 LIBDIR = os.path.join(PKG_DIR, "nbody_gb300")
 NVCC = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"

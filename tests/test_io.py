@@ -5,7 +5,9 @@ import os
 import numpy as np
 import pytest
 
-REF_PARTICLES = os.path.join(os.environ.get("REF_ROOT", "/root/reference"), "particles_100.txt")
+from conftest import ref_root
+
+REF_PARTICLES = os.path.join(ref_root() or "", "particles_100.txt")
 
 
 def test_particles_round_trip_bit_exact(nb, tmp_path):
@@ -29,7 +31,8 @@ def test_particles_empty_file_has_zero_bodies(nb, tmp_path):
     assert all(len(v) == 0 for v in out)
 
 
-@pytest.mark.parametrize("text", ["", "abc\n", "3\n1 2 3 4 5 6 7\n1 2 3\n", "-2\n"])
+@pytest.mark.parametrize("text", ["", "abc\n", "3\n1 2 3 4 5 6 7\n1 2 3\n", "-2\n", "2.5\n",
+                                  "1e30\n", "nan\n", "inf\n"])
 def test_particles_malformed_is_io_error(nb, tmp_path, text):
     p = tmp_path / "bad.txt"
     p.write_text(text)
@@ -56,7 +59,8 @@ def test_particles_capacity_error(nb, tmp_path):
     assert st == 4 and n.value == 3
 
 
-@pytest.mark.skipif(not os.path.exists(REF_PARTICLES), reason="reference fixtures absent")
+@pytest.mark.skipif(not ref_root() or not os.path.exists(REF_PARTICLES),
+                    reason="reference checkout not located (REF_ROOT)")
 def test_reads_reference_fixture_like_its_loader(nb):
     """Same values as a whitespace-split parse (the reference's `file >> ...`)."""
     tok = open(REF_PARTICLES).read().split()

@@ -227,3 +227,16 @@ def test_split_levels(oracle):
     assert oracle.split_levels(200.0) == 21
     assert oracle.split_levels(1e-8) == 3   # 1e-8/2^3 = 1.25e-9 >= 1e-9 > 6.25e-10
     assert oracle.split_levels(1e-9) == 0
+
+
+@pytest.mark.parametrize("kind,n,seed", [("plummer", 1, 0), ("plummer", 4097, 3),
+                                         ("plummer", 65536, 0), ("disk_bulge", 5, 1),
+                                         ("disk_bulge", 20000, 8)])
+def test_oracle_generators_match_the_engine(oracle, nb, kind, n, seed):
+    """The oracle's restated workload generators give the engine's bits, so
+    the CPU arms of the benchmark build the same inputs without loading the
+    engine library."""
+    a = getattr(oracle, kind)(n, seed)
+    b = getattr(nb, kind)(n, seed)
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)
