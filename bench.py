@@ -69,12 +69,16 @@ def parse():
     ap.add_argument("--ens-steps", type=int, default=25,
                     help="RK4 steps of the 4096-system ensemble extra (0 skips it)")
     ap.add_argument("--ens-systems", type=int, default=4096)
-    ap.add_argument("--serve-seconds", type=float, default=1.0,
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="seconds of Poisson arrivals for the serving extra (0 skips it)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
-    ap.add_argument("--drift-steps", type=int, default=200,
+    ap.add_argument("--drift-steps", type=int, default=1000,
                     help="velocity-Verlet steps of the mixed vs FP64 energy-drift comparison "
                          "(0 skips it; the target is stated over 1000)")
+    ap.add_argument("--no-bh-cpu", dest="bh_cpu", action="store_false",
+                    help="skip the CPU Barnes-Hut evaluation of the Barnes-Hut extra")
+    ap.add_argument("--no-ens-cpu", dest="ens_cpu", action="store_false",
+                    help="skip the CPU RK4 sample of the ensemble extra")
     ap.add_argument("--only", choices=["bh", "ensemble", "serving"], default=None,
                     help="run one extra workload alone and print its record (profiling)")
     return ap.parse_args()
@@ -192,6 +196,25 @@ def load_oracle():
     return O
 
 
+def host_cpu():
+    """The host CPU's model name and the number of threads the oracle uses."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if model is None and os.path.exists("/proc/cpuinfo"):
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                model = line.split(":", 1)[1].strip()
+                break
+    return {"cpu_model": model or "unknown", "host_threads": os.cpu_count()}
+
+
 def cpu_reference_rate(n, target_seconds, threads=0):
     """The reference's FP64 direct sum on the host cores (its C restatement),
     timed on a bounded sample of i-rows of the same workload.  The inputs come
@@ -235,6 +258,18 @@ def run_plain(nb, torch, stream):
                    "steps": steps, "ms_per_step": ms, "steps_per_s": 1e3 / ms,
                    "ginteractions_s": n * (n - 1) / (ms / 1e3) / 1e9,
                    "energy_rel_change": (e1 - e0) / abs(e0)}
+    # the reference's CPU path on the same configuration: its leapfrog
+    # integrator with the direct sum (two force evaluations per step), the
+    # whole 100-step run (C restatement, all host threads)
+    O = load_oracle()
+    t0 = time.perf_counter()
+    O.run(O.LEAPFROG, O.DIRECT, *state, 1.0, 0.01, 1e-3, steps)
+    el = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": steps / el, "unit": "steps/s", "kind": "port",
+                           "cores": O.threads(), "ms_per_step": el / steps * 1e3,
+                           "sample": f"the whole run: {steps} leapfrog steps of N = {n}, "
+                                     "FP64 direct sum", **host_cpu()}
+    out["speedup_vs_cpu"] = out["steps_per_s"] / out["cpu_baseline"]["value"]
     return out
 
 
@@ -343,7 +378,7 @@ def run_reference(a, rank, world):
         "config": {"workload": WORKLOAD, "n": n, "softening": EPS, "dt": DT,
                    "integrator": "velocity_verlet", "method": "direct_fp64_cpu"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, **host_cpu()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
@@ -438,6 +473,26 @@ def run_bh(a, nb, torch, dev, stream, flush, np):
     if "quad" in variants:
         quad = timed(nb.BH_QUADRUPOLE)
         out["quadrupole"] = {k: quad[k] for k in keys}
+    if a.bh_cpu:
+        out["cpu_baseline"] = bh_cpu_baseline(state, out.get("ms_per_step"))
+    return out
+
+
+def bh_cpu_baseline(state, gpu_ms_per_step):
+    """The reference's CPU Barnes-Hut (ForceCalculatorBarnesHutOptimized, leaf
+    capacity 8, theta 0.5: its C restatement, serial build + walk over all host
+    threads) timed on one force evaluation of the same bodies."""
+    O = load_oracle()
+    x, y, z, m = state[0], state[1], state[2], state[6]
+    t0 = time.perf_counter()
+    O.forces_bh_opt(x, y, z, m, 1.0, EPS, BH_THETA, 8)
+    el = time.perf_counter() - t0
+    out = {"value": 1.0 / el, "unit": "force evaluations/s", "kind": "port",
+           "cores": O.threads(), "s_per_eval": el,
+           "sample": f"one force evaluation of all {len(x)} bodies (node-pool tree, leaf 8, "
+                     f"theta {BH_THETA})", **host_cpu()}
+    if gpu_ms_per_step:
+        out["gpu_step_speedup"] = el / (gpu_ms_per_step / 1e3)
     return out
 
 
@@ -470,6 +525,7 @@ def run_ensemble(a, nb, torch, stream):
     e.close()
     inter = info["interactions_per_eval"]
     kernel_ms = pinfo["force_kernel_ms"] / max(1, pinfo["force_launches"])
+    cpu = ensemble_cpu_baseline(a, sizes, state, inter, ms) if a.ens_cpu else None
     return {"workload": f"{a.ens_systems}_plummer_systems_n32_4096_rk4",
             "systems": a.ens_systems, "bodies": int(sizes.sum()),
             "interactions_per_eval": inter, "steps": a.ens_steps, "ms_per_step": ms,
@@ -478,7 +534,41 @@ def run_ensemble(a, nb, torch, stream):
             "force_kernel_ginteractions_s": inter / (kernel_ms / 1e3) / 1e9,
             "work_items": info["work_items"], "graph_steps_per_replay": info["graph_steps"],
             "ipt_by_bucket": {str(b): info["ipt_by_bucket"][b] for b in range(5, 13)},
-            "timing": "CUDA events around the graph-replayed step loop"}
+            "timing": "CUDA events around the graph-replayed step loop",
+            "cpu_baseline": cpu}
+
+
+def ensemble_cpu_baseline(a, sizes, state, inter, gpu_ms_per_step):
+    """The reference's CPU RK4 integrator with the direct sum (four force
+    evaluations per step; its C restatement over all host threads): one step of
+    every k-th system, k chosen so that the sample holds about a.cpu_seconds of
+    work, scaled to the whole ensemble by its sum of N (N - 1)."""
+    import numpy as np
+    O = load_oracle()
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    per_sys = sizes.astype(np.float64) * (sizes - 1)
+    # calibrate on the largest system
+    big = int(np.argmax(sizes))
+    sl = slice(int(offs[big]), int(offs[big + 1]))
+    t0 = time.perf_counter()
+    O.run(O.RK4, O.DIRECT, *(v[sl] for v in state), 1.0, EPS, 1e-3, 1)
+    rate = 4 * per_sys[big] / max(time.perf_counter() - t0, 1e-6)
+    want = rate * a.cpu_seconds / 4.0
+    stride = max(1, int(np.ceil(per_sys.sum() / max(want, 1.0))))
+    picked = list(range(0, len(sizes), stride))
+    t0 = time.perf_counter()
+    for s_ in picked:
+        sl = slice(int(offs[s_]), int(offs[s_ + 1]))
+        O.run(O.RK4, O.DIRECT, *(v[sl] for v in state), 1.0, EPS, 1e-3, 1)
+    el = time.perf_counter() - t0
+    done = 4 * per_sys[picked].sum()
+    gint = done / el / 1e9
+    full_step_s = 4 * inter / (gint * 1e9)
+    return {"value": gint, "unit": UNIT, "kind": "port", "cores": O.threads(),
+            "sample": f"one RK4 step of every {stride}-th system ({len(picked)} of {len(sizes)}"
+                      f" systems, {done:.3g} interactions), FP64 direct sum",
+            "full_ensemble_s_per_step": full_step_s,
+            "gpu_step_speedup": full_step_s / (gpu_ms_per_step / 1e3), **host_cpu()}
 
 
 # ---------------------------------------------------------------- serving
@@ -705,7 +795,7 @@ def run_ours(a, rank, world, local_rank):
         el = time.perf_counter() - t0
         cpu = {"value": rows * (n - 1) / el / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"FP64 direct sum of the reference (C restatement), {rows} of {n} "
-                         f"i-rows x all {n} j, one pass"}
+                         f"i-rows x all {n} j, one pass", **host_cpu()}
     sim.close()
     if world > 1:
         torch.distributed.barrier()
@@ -728,8 +818,36 @@ def run_ours(a, rank, world, local_rank):
         "clocks": clk,
     }
     line.update(extras)
+    line["summary"] = summarize(line)
     print(json.dumps(line), flush=True)
     return 0
+
+
+def summarize(line):
+    """The figures a reader looks for first, repeated at the end of the line."""
+    def get(*keys):
+        v = line
+        for k in keys:
+            if not isinstance(v, dict) or k not in v or v[k] is None:
+                return None
+            v = v[k]
+        return v
+    return {
+        "gint_s": line["value"], "e2e_gint_s": get("e2e", "value"),
+        "roofline_frac": get("roofline", "frac"),
+        "force_err_max_rel": get("force_error_vs_fp64", "max_rel"),
+        "force_err_rms_rel": get("force_error_vs_fp64", "rms_rel"),
+        "mixed_over_fp64_gpu": get("fp64_direct", "mixed_speedup"),
+        "mixed_over_reference_gpu_kernel": get("gpu_baseline", "mixed_kernel_speedup"),
+        "drift_ratio_mixed_over_fp64": get("energy_drift_vs_fp64", "ratio_mixed_over_fp64"),
+        "drift_steps": get("energy_drift_vs_fp64", "steps"),
+        "bh_steps_per_s": get("barnes_hut", "steps_per_s"),
+        "bh_cpu_s_per_eval": get("barnes_hut", "cpu_baseline", "s_per_eval"),
+        "ensemble_gint_s": get("ensemble", "ginteractions_s"),
+        "serving_p50_p99_ms": [get("serving", "step_ms_p50"), get("serving", "step_ms_p99")],
+        "serving_gint_s": get("serving", "ginteractions_s"),
+        "cpu_baseline_gint_s": get("cpu_baseline", "value"),
+    }
 
 
 def run_only(a, local_rank):

@@ -341,7 +341,7 @@ bool launch_mixed(const DirectPlan &p, cudaStream_t st, const float4 *hi, const 
     return true;
 }
 
-DirectPlan plan_for_shape(int n, int block, int ipt)
+DirectPlan plan_for_shape_model(int n, int block, int ipt)
 {
     DirectPlan p;
     p.block = block;
@@ -352,6 +352,29 @@ DirectPlan plan_for_shape(int n, int block, int ipt)
     p.segments = pick_segments(iblocks, tiles, mix_slots_for(block, ipt));
     p.seg_tiles = (tiles + p.segments - 1) / p.segments;
     p.segments = (tiles + p.seg_tiles - 1) / p.seg_tiles;
+    return p;
+}
+
+// The j-segment length of n bodies: that of the default shape (one-warp CTAs
+// below 4096 bodies, kMixBlock x kMixIpt above).  A body's summation order
+// depends only on the segment boundaries (every shape sums each segment in
+// 32-body tiles from its start), so fixing them per n makes every tile shape
+// give the same bits and the autotuner's timed choice cannot change a result.
+int mixed_segment_length(int n)
+{
+    const DirectPlan d = n < 4096 ? plan_for_shape_model(n, 32, n < 2048 ? 1 : 2)
+                                  : plan_for_shape_model(n, kMixBlock, kMixIpt);
+    return d.seg_tiles * d.block;
+}
+
+DirectPlan plan_for_shape(int n, int block, int ipt)
+{
+    DirectPlan p;
+    p.block = block;
+    p.ipt = ipt;
+    const int seg_len = mixed_segment_length(n);  // a multiple of every block size below it
+    p.seg_tiles = std::max(1, seg_len / block);
+    p.segments = std::max(1, (n + seg_len - 1) / seg_len);
     return p;
 }
 

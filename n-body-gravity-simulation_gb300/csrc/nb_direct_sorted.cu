@@ -83,9 +83,10 @@ __global__ void split_sorted_kernel(const uint32_t *__restrict__ order,
         const double X = x[o] - centre[0], Y = y[o] - centre[1], Z = z[o] - centre[2];
         const float hx = __double2float_rn(X), hy = __double2float_rn(Y),
                     hz = __double2float_rn(Z);
-        hi[i] = make_float4(hx, hy, hz, __double2float_rn(m[o]));
+        const float hm = __double2float_rn(m[o]);
+        hi[i] = make_float4(hx, hy, hz, hm);
         lo[i] = make_float4(__double2float_rn(X - (double)hx), __double2float_rn(Y - (double)hy),
-                            __double2float_rn(Z - (double)hz), 0.0f);
+                            __double2float_rn(Z - (double)hz), __double2float_rn(m[o] - (double)hm));
         p[0] = hx;
         p[1] = hy;
         p[2] = hz;
@@ -119,7 +120,7 @@ __global__ void __launch_bounds__(WARPS * 32)
 direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                      const float4 *__restrict__ box, int n, int nchunks, float eps2,
                      int seg_chunks, float *__restrict__ psum, float *__restrict__ pcomp,
-                     float far2)
+                     float far2, double eps2d)
 {
     __shared__ PairTile stage[WARPS];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -143,6 +144,20 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
                         (bmx[2] - bmn[2]) * (bmx[2] - bmn[2]);
     const float thr2 = far2 * diam2;           // far: double-single not needed
     const float thr2v = kVeryFar2 * diam2;     // very far: Newton step not needed
+    // Pairs closer than R leave the FP32 sum and are evaluated in double-single
+    // (only chunks nearer than R can hold one): R = min(kExact D, kExactSpacing
+    // s), s the mean body spacing of the warp's box, (V / 64)^(1/3) with every
+    // side padded by D / 16 so that a flat box keeps its in-plane spacing.  The
+    // spacing cap keeps sparse warps with large boxes from sending many pairs.
+    float thr2x;
+    {
+        const float pad = 0.0625f * sqrtf(diam2);
+        const float vol = (bmx[0] - bmn[0] + pad) * (bmx[1] - bmn[1] + pad) * (bmx[2] - bmn[2] + pad);
+        const float s2 = exp2f(0.6666667f * log2f(vol * (1.0f / (32.0f * IPT))));
+        thr2x = fminf(kExact2 * diam2, kExactSpacing2 * s2);
+    }
+    const float thrx = __fadd_rn(thr2x, eps2);
+    const DS e2ds{__double2float_rn(eps2d), __double2float_rn(eps2d - (double)__double2float_rn(eps2d))};
 
     // i-bodies relative to c, negated and duplicated into pairs
     float2 nsx[IPT], nsy[IPT], nsz[IPT], nex[IPT], ney[IPT], nez[IPT];
@@ -189,6 +204,7 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
         const float gap2 = gx * gx + gy * gy + gz * gz;
         const bool far = gap2 > 0.f && gap2 >= thr2;
         const bool vfar = far && gap2 >= thr2v;
+        const bool touch = !far && gap2 < thr2x;
 
         // lanes past n stage a massless body far away: its terms are exactly 0
         float Sx = 1.0e18f, Sy = 1.0e18f, Sz = 1.0e18f, Ex = 0.f, Ey = 0.f, Ez = 0.f, mj = 0.f;
@@ -209,6 +225,7 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
             pair_tile_put_hi(sg, lane, Sx, Sy, Sz, mj);
         else
             pair_tile_put(sg, lane, Sx, Sy, Sz, mj, Ex, Ey, Ez);
+        if (touch) pair_tile_put_mlo(sg, lane, valid ? l.w : 0.f);
         __syncwarp();
         valid = jc + 1 < jc1 && (jc + 1) * kChunk + lane < n;
         if (valid) {
@@ -231,6 +248,42 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
 #pragma unroll
                 for (int k = 0; k < IPT; ++k)
                     pair_term2_far<true>(j, nsx[k], nsy[k], nsz[k], e2, ax[k], ay[k], az[k]);
+            }
+        } else if (touch) {
+            bool hit = false;
+#pragma unroll 4
+            for (int p = 0; p < kChunk / 2; ++p) {
+                const JPair j = pair_tile_get(sg, p);
+#pragma unroll
+                for (int k = 0; k < IPT; ++k)
+                    pair_term2_excl<ZERO_SOFT>(j, nsx[k], nsy[k], nsz[k], nex[k], ney[k], nez[k],
+                                               e2, thrx, ax[k], ay[k], az[k], hit);
+            }
+            if (__any_sync(0xffffffffu, hit)) {
+                // the same r^2 again (same operands, same bits): the lane's
+                // left-out pairs in double-single, its own body (j == i) excepted
+#pragma unroll 1
+                for (int p = 0; p < kChunk / 2; ++p) {
+                    const JPair j = pair_tile_get(sg, p);
+                    const float2 mlo = sg.g[p];
+                    const int j0 = jc * kChunk + 2 * p;
+#pragma unroll
+                    for (int k = 0; k < IPT; ++k) {
+                        const PairGeom g =
+                            pair_geom(j, nsx[k], nsy[k], nsz[k], nex[k], ney[k], nez[k], e2);
+                        const int i = (tile0 + k) * kChunk + lane;
+                        const DS xi{-nsx[k].x, -nex[k].x}, yi{-nsy[k].x, -ney[k].x},
+                            zi{-nsz[k].x, -nez[k].x};
+                        if (g.r2.x < thrx && i < n && j0 != i)
+                            pair_term_ds(DS{j.x.x, j.xl.x}, DS{j.y.x, j.yl.x}, DS{j.z.x, j.zl.x},
+                                         DS{j.m.x, mlo.x}, xi, yi, zi, e2ds, sx[k], qx[k], sy[k],
+                                         qy[k], sz[k], qz[k]);
+                        if (g.r2.y < thrx && i < n && j0 + 1 != i)
+                            pair_term_ds(DS{j.x.y, j.xl.y}, DS{j.y.y, j.yl.y}, DS{j.z.y, j.zl.y},
+                                         DS{j.m.y, mlo.y}, xi, yi, zi, e2ds, sx[k], qx[k], sy[k],
+                                         qy[k], sz[k], qz[k]);
+                    }
+                }
             }
         } else {
 #pragma unroll 4
@@ -299,10 +352,13 @@ __global__ void combine_sorted_kernel(const float *__restrict__ psum,
 // Warps stage their own j-chunks, so the CTA size matters only for
 // scheduling: with one- or two-warp CTAs a slow warp (many near chunks) holds
 // fewer idle warp slots until its CTA retires (1.2 % faster at N = 65,536).
+// Chunks per warp (the warp's box, hence its near/far decisions and origin)
+// and the j-segments (sorted_plan_for_shape) are the same for every shape, so
+// the timed choice never changes the bits of a result.
 struct SortedShape {
     int warps, ipt;
 };
-constexpr SortedShape kSortedShapes[] = {{4, 4}, {8, 4}, {4, 2}, {8, 2}, {2, 2}, {1, 2}};
+constexpr SortedShape kSortedShapes[] = {{4, 2}, {8, 2}, {2, 2}, {1, 2}};
 constexpr int kNumSortedShapes = sizeof(kSortedShapes) / sizeof(kSortedShapes[0]);
 
 template <int W, int I>
@@ -319,8 +375,6 @@ int sorted_slots()
 
 int sorted_slots_for(int warps, int ipt)
 {
-    if (warps == 4 && ipt == 4) return sorted_slots<4, 4>();
-    if (warps == 8 && ipt == 4) return sorted_slots<8, 4>();
     if (warps == 4 && ipt == 2) return sorted_slots<4, 2>();
     if (warps == 8 && ipt == 2) return sorted_slots<8, 2>();
     if (warps == 2 && ipt == 2) return sorted_slots<2, 2>();
@@ -336,10 +390,10 @@ void launch_sorted_shape(dim3 grid, cudaStream_t st, const float4 *hi, const flo
     const int nchunks = (n + kChunk - 1) / kChunk;
     if (eps2 > 0.0)
         direct_sorted_kernel<W, I, false><<<grid, W * 32, 0, st>>>(
-            hi, lo, box, n, nchunks, (float)eps2, seg_chunks, psum, pcomp, kFarFactor2);
+            hi, lo, box, n, nchunks, (float)eps2, seg_chunks, psum, pcomp, kFarFactor2, eps2);
     else
         direct_sorted_kernel<W, I, true><<<grid, W * 32, 0, st>>>(
-            hi, lo, box, n, nchunks, 0.0f, seg_chunks, psum, pcomp, kFarFactor2);
+            hi, lo, box, n, nchunks, 0.0f, seg_chunks, psum, pcomp, kFarFactor2, 0.0);
 }
 
 // DirectPlan fields here: block = threads per CTA (32 * warps), ipt = chunks
@@ -351,11 +405,7 @@ bool launch_sorted(const DirectPlan &p, cudaStream_t st, const float4 *hi, const
     const int nchunks = (n + kChunk - 1) / kChunk;
     const int per_cta = warps * p.ipt;
     const dim3 grid((nchunks + per_cta - 1) / per_cta, p.segments);
-    if (warps == 4 && p.ipt == 4)
-        launch_sorted_shape<4, 4>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
-    else if (warps == 8 && p.ipt == 4)
-        launch_sorted_shape<8, 4>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
-    else if (warps == 4 && p.ipt == 2)
+    if (warps == 4 && p.ipt == 2)
         launch_sorted_shape<4, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
     else if (warps == 8 && p.ipt == 2)
         launch_sorted_shape<8, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
@@ -368,17 +418,17 @@ bool launch_sorted(const DirectPlan &p, cudaStream_t st, const float4 *hi, const
     return true;
 }
 
+// The j-split is modelled on one-warp CTAs of two chunks for every shape
+// (segments of at least 8 chunks, 256 j), so it depends on n alone.
 DirectPlan sorted_plan_for_shape(int n, int warps, int ipt)
 {
     DirectPlan p;
     p.block = warps * 32;
     p.ipt = ipt;
     const int nchunks = (n + kChunk - 1) / kChunk;
-    const int per_cta = warps * ipt;
-    const int iblocks = (nchunks + per_cta - 1) / per_cta;
-    // segments of at least 8 chunks (256 j)
+    const int iblocks = (nchunks + 1) / 2;
     const int units = std::max(1, nchunks / 8);
-    const int s = direct_pick_segments(iblocks, units, sorted_slots_for(warps, ipt));
+    const int s = direct_pick_segments(iblocks, units, sorted_slots_for(1, 2));
     p.seg_tiles = (nchunks + s - 1) / s;
     p.segments = (nchunks + p.seg_tiles - 1) / p.seg_tiles;
     return p;
@@ -426,11 +476,9 @@ static nb_status run_sorted(const DirectPlan &p, const float4 *hi, const float4 
     return NB_OK;
 }
 
-// Times every CTA shape, each with the modelled j-split and with 1.5 times as
-// many segments (shorter CTAs balance better at the end of the launch but
-// give the combine more partials to read), kernel and combine together (the
-// combine writes the real outputs, which the evaluation then overwrites), and
-// records the fastest plan for this n.
+// Times every CTA shape, kernel and combine together (the combine writes the
+// real outputs, which the evaluation then overwrites), and records the
+// fastest plan for this n.
 static nb_status autotune_sorted(const float4 *hi, const float4 *lo, int n, double eps2,
                                  double G, const uint32_t *order, double *ax, double *ay,
                                  double *az, SortedBuffers &b, cudaStream_t st, DirectPlan *best)
@@ -442,20 +490,9 @@ static nb_status autotune_sorted(const float4 *hi, const float4 *lo, int n, doub
     // Above 2^18 bodies every shape is timed on all i-bodies against the first
     // 512 j-chunks only (one segment): an evaluation there takes 0.1 s and more.
     const bool probe = n > (1 << 18);
-    const int nchunks = (n + kChunk - 1) / kChunk;
     for (int k = 0; k < kNumSortedShapes; ++k) {
-        const DirectPlan p0 = sorted_plan_for_shape(n, kSortedShapes[k].warps, kSortedShapes[k].ipt);
-        DirectPlan variants[2] = {p0, p0};
-        int num_variants = 1;
-        if (!probe) {
-            const int s1 = (3 * p0.segments + 1) / 2;
-            DirectPlan &v = variants[1];
-            v.seg_tiles = std::max(1, (nchunks + s1 - 1) / s1);
-            v.segments = (nchunks + v.seg_tiles - 1) / v.seg_tiles;
-            if (v.segments != p0.segments) num_variants = 2;
-        }
-        for (int vi = 0; vi < num_variants; ++vi) {
-            const DirectPlan &p = variants[vi];
+        const DirectPlan p = sorted_plan_for_shape(n, kSortedShapes[k].warps, kSortedShapes[k].ipt);
+        {
             DirectPlan t = p;
             if (probe) {
                 t.segments = 1;
@@ -467,8 +504,8 @@ static nb_status autotune_sorted(const float4 *hi, const float4 *lo, int n, doub
             for (int r = 0; r < 2; ++r) {
                 NB_TRY(run_sorted(t, hi, lo, n, eps2, b, st, &psum));
                 combine_sorted_kernel<<<(n + 255) / 256, 256, 0, st>>>(
-                    psum, psum + 3 * (size_t)n * t.segments, n, t.segments, G, order, ax, ay,
-                    az);
+                    psum, psum + 3 * (size_t)n * t.segments, n, t.segments, G, order, ax,
+                    ay, az);
                 NB_LAUNCH_CHECK();
             }
             cudaEventRecord(e1, st);
@@ -527,7 +564,7 @@ nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
         const char *e = std::getenv("NB_AUTOTUNE");
         if (!(e && std::strcmp(e, "0") == 0))
             NB_TRY(autotune_sorted(hi, lo, n, eps2, G, order, ax, ay, az, b, st, &p));
-        else p = sorted_plan_for_shape(n, 4, 4);
+        else p = sorted_plan_for_shape(n, 1, 2);
     }
     if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
     float *psum = nullptr;

@@ -110,6 +110,12 @@ int direct_pick_segments(int iblocks, int tiles, int slots);
 // 1/4).
 constexpr float kFarFactor2 = 0.015625f;
 constexpr float kVeryFar2 = 0.0625f;
+// Pairs of the sorted single-system kernel closer than R = min(kExact D,
+// kExactSpacing s) (s: the mean body spacing in the warp's box) leave its FP32
+// sum and are evaluated in double-single: they carry the largest terms of a
+// body's sum, whose FP32 rounding would otherwise set its error.
+constexpr float kExact2 = 0.015625f;        // kExact = 1/8
+constexpr float kExactSpacing2 = 0.5625f;   // kExactSpacing = 3/4
 
 // Hilbert-sorted near/far variant of the mixed path (nb_direct_sorted.cu).
 struct BHTree;

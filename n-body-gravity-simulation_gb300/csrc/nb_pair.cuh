@@ -131,6 +131,7 @@ struct PairTile {
     float4 t[16];  // (z_2p, z_2p+1, m_2p, m_2p+1)
     float4 e[16];  // (xlo_2p, xlo_2p+1, ylo_2p, ylo_2p+1)
     float2 f[16];  // (zlo_2p, zlo_2p+1)
+    float2 g[16];  // (mlo_2p, mlo_2p+1): mass low parts, written by pair_tile_put_mlo
 };
 
 // Lane `lane` writes its j-body into the tile (call between two __syncwarp).
@@ -148,6 +149,12 @@ __device__ __forceinline__ void pair_tile_put(PairTile &pt, int lane, float x, f
     e[0] = xl;
     e[2] = yl;
     f[0] = zl;
+}
+
+// Lane `lane`'s mass low part (m - (float)m), for the double-single terms.
+__device__ __forceinline__ void pair_tile_put_mlo(PairTile &pt, int lane, float ml)
+{
+    reinterpret_cast<float *>(&pt.g[lane >> 1])[lane & 1] = ml;
 }
 
 // The same without the low parts (a tile read only by pair_term2_far).
@@ -180,21 +187,136 @@ __device__ __forceinline__ JPair pair_tile_get(const PairTile &pt, int p)
     return j;
 }
 
-// The double-single pair term of pair_term for a j-pair against one i-body
-// given as negated duplicated pairs (nxh = (-xh, -xh), ...).
+// Double-single displacement and softened r^2 of a j-pair against one i-body
+// given as negated duplicated pairs (nxh = (-xh, -xh), ...).  Every operation
+// is an explicit round-to-nearest intrinsic, so two evaluations of the same
+// operands give the same bits (the near-pair exclusion below relies on it).
+struct PairGeom {
+    float2 dx, dy, dz, r2;
+};
+__device__ __forceinline__ PairGeom pair_geom(const JPair &j, float2 nxh, float2 nyh, float2 nzh,
+                                              float2 nxl, float2 nyl, float2 nzl, float2 e2)
+{
+    PairGeom g;
+    g.dx = add2(add2(j.x, nxh), add2(j.xl, nxl));
+    g.dy = add2(add2(j.y, nyh), add2(j.yl, nyl));
+    g.dz = add2(add2(j.z, nzh), add2(j.zl, nzl));
+    g.r2 = fma2(g.dz, g.dz, fma2(g.dy, g.dy, fma2(g.dx, g.dx, e2)));
+    return g;
+}
+
+// The double-single pair term of pair_term for a j-pair against one i-body.
 template <bool ZERO_SOFT>
 __device__ __forceinline__ void pair_term2(const JPair &j, float2 nxh, float2 nyh, float2 nzh,
                                            float2 nxl, float2 nyl, float2 nzl, float2 e2,
                                            float2 &ax, float2 &ay, float2 &az)
 {
-    const float2 dx = add2(add2(j.x, nxh), add2(j.xl, nxl));
-    const float2 dy = add2(add2(j.y, nyh), add2(j.yl, nyl));
-    const float2 dz = add2(add2(j.z, nzh), add2(j.zl, nzl));
-    const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
-    const float2 s = pair_scale<ZERO_SOFT>(r2, j.m);
-    ax = fma2(dx, s, ax);
-    ay = fma2(dy, s, ay);
-    az = fma2(dz, s, az);
+    const PairGeom g = pair_geom(j, nxh, nyh, nzh, nxl, nyl, nzl, e2);
+    const float2 s = pair_scale<ZERO_SOFT>(g.r2, j.m);
+    ax = fma2(g.dx, s, ax);
+    ay = fma2(g.dy, s, ay);
+    az = fma2(g.dz, s, az);
+}
+
+// pair_term2 for the pairs closer than a threshold: a lane whose r^2 (with
+// the softening) is below thr adds nothing here and sets `hit`; the caller
+// evaluates those pairs in double-single instead (pair_term_ds).  Such pairs carry the largest
+// terms of a body's sum, so the FP32 rounding of their term and of the
+// partial sums that hold them would dominate its error.
+template <bool ZERO_SOFT>
+__device__ __forceinline__ void pair_term2_excl(const JPair &j, float2 nxh, float2 nyh,
+                                                float2 nzh, float2 nxl, float2 nyl, float2 nzl,
+                                                float2 e2, float thr, float2 &ax, float2 &ay,
+                                                float2 &az, bool &hit)
+{
+    const PairGeom g = pair_geom(j, nxh, nyh, nzh, nxl, nyl, nzl, e2);
+    float2 s = pair_scale<ZERO_SOFT>(g.r2, j.m);
+    const bool h0 = g.r2.x < thr, h1 = g.r2.y < thr;
+    s.x = h0 ? 0.f : s.x;
+    s.y = h1 ? 0.f : s.y;
+    hit = hit || h0 || h1;
+    ax = fma2(g.dx, s, ax);
+    ay = fma2(g.dy, s, ay);
+    az = fma2(g.dz, s, az);
+}
+
+// ---------------------------------------------------------------- double-single
+// The pairs that leave the FP32 sum (pair_term2_excl) are evaluated in
+// double-single arithmetic: an unevaluated sum hi + lo of two FP32 values,
+// about 48 significant bits, built from error-free transformations (Knuth's
+// two-sum, and the FMA product split).  On the FP32 pipe this costs a few
+// dozen instructions per pair, far less than the few FP64 operations GB300's
+// narrow FP64 pipe can issue per clock.
+struct DS {
+    float hi, lo;
+};
+
+// hi + lo with |lo| <= ulp(hi) / 2 (requires |a| >= |b| or a == 0).
+__device__ __forceinline__ DS quick_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    return DS{s, __fadd_rn(b, -__fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ DS ds_add(DS a, DS b)
+{
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    return quick_two_sum(s, e);
+}
+
+__device__ __forceinline__ DS ds_mul(DS a, DS b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);  // exact rounding error of the product
+    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    return quick_two_sum(p, e);
+}
+
+// (a - b) of two normalised double-singles, exact to their ~2^-48 resolution.
+__device__ __forceinline__ DS ds_sub(DS a, DS b) { return ds_add(a, DS{-b.hi, -b.lo}); }
+
+// 1 / sqrt(x) for x > 0: the MUFU estimate y0 (~1.3e-7) and one Newton step
+// whose residual 1 - x y0^2 is formed in double-single, leaving an error of
+// order 1e-14.
+__device__ __forceinline__ DS ds_rsqrt(DS x)
+{
+    const float y0 = rsqrt_mufu(x.hi);
+    const DS y0s{y0, 0.f};
+    const DS t = ds_mul(ds_mul(x, y0s), y0s);
+    const float h = __fadd_rn(__fsub_rn(1.0f, t.hi), -t.lo);  // 1 - x y0^2, ~1e-7
+    return quick_two_sum(y0, __fmul_rn(__fmul_rn(0.5f, y0), h));
+}
+
+// (s, c) += v for a Kahan pair (value s - c) and a double-single v of any
+// magnitude: v.hi joins s through an exact two-sum (Kahan's own update
+// assumes |s| >= |v|, which a dominant term breaks), so the pair keeps about
+// 48 bits of the sum.
+__device__ __forceinline__ void kahan_add_ds(float &s, float &c, DS v)
+{
+    float S, E;
+    two_sum(s, v.hi, S, E);
+    s = S;
+    c = __fsub_rn(__fsub_rn(c, E), v.lo);
+}
+
+// The pair term m_j (r_j - r_i) / (|r_j - r_i|^2 + eps2)^(3/2) in
+// double-single from the double-single coordinates (relative to a common
+// origin) and mass of both bodies; added into the Kahan pairs (sx, cx) ...
+// with kahan_add_ds.  r2 == 0 (coincident bodies, no softening) adds nothing.
+__device__ __forceinline__ void pair_term_ds(DS xj, DS yj, DS zj, DS mj, DS xi, DS yi, DS zi,
+                                             DS eps2, float &sx, float &cx, float &sy,
+                                             float &cy, float &sz, float &cz)
+{
+    const DS dx = ds_sub(xj, xi), dy = ds_sub(yj, yi), dz = ds_sub(zj, zi);
+    const DS r2 = ds_add(ds_add(ds_mul(dx, dx), ds_mul(dy, dy)), ds_add(ds_mul(dz, dz), eps2));
+    if (!(r2.hi > 0.f)) return;
+    const DS y = ds_rsqrt(r2);
+    const DS sc = ds_mul(mj, ds_mul(ds_mul(y, y), y));
+    kahan_add_ds(sx, cx, ds_mul(sc, dx));
+    kahan_add_ds(sy, cy, ds_mul(sc, dy));
+    kahan_add_ds(sz, cz, ds_mul(sc, dz));
 }
 
 // The plain FP32 term (coordinates already relative to a nearby origin).

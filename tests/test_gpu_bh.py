@@ -358,3 +358,54 @@ def test_quadrupole_with_tree_reuse(nb):
             errs.append(float(np.mean(d / np.sqrt(sum(v * v for v in a_ref)))))
     # refit evaluations (2-4) as accurate as the build (1)
     assert max(errs) <= 1.15 * errs[0], errs
+
+
+def test_configuration_size_disk_bulge_2_20(nb, oracle):
+    """The Barnes-Hut configuration itself: N = 2^20 Plummer bulge + exponential
+    disk (the benchmark's bodies, generator seed 0), leaf 8, theta 0.5, eps
+    1e-3.  Its deep chains (12 levels) and 444k nodes stress the encode's
+    exact fast path and the gallop build hardest.
+      - Morton codes, sort order and the whole node table are bit-exact
+        against the oracle;
+      - forces of 2048 sampled bodies against the oracle's FP64 direct sum:
+        the mean relative error is no worse than that of the reference's CPU
+        node-pool tree (CPU/src/force_calculator_barnes_hut_optimized.cpp,
+        restated in the oracle) on the same input, and the 99th percentile is
+        within 1.5x of the CPU tree's."""
+    n, leaf, theta, eps = 1 << 20, 8, 0.5, 1e-3
+    state = nb.disk_bulge(n, seed=0)
+    x, y, z, m = state[0], state[1], state[2], state[6]
+    sc, order, t, root, levels = oracle_tree(oracle, x, y, z, leaf)
+    with bh_sim(nb, state, eps=eps, theta=theta, leaf=leaf) as s:
+        info = s.bh_build()
+        codes, gorder = s.bh_order()
+        assert info["root"] == list(root)
+        assert np.array_equal(codes, sc)
+        assert np.array_equal(gorder, order)
+        nodes = s.bh_nodes(info["num_nodes"])
+        s.compute_forces()
+        a = s.accelerations()
+    assert info["num_nodes"] == len(t["depth"])
+    got = np.lexsort((nodes["is_leaf"], nodes["count"], nodes["first"], nodes["prefix"],
+                      nodes["depth"]))
+    want = np.lexsort((t["is_leaf"], t["count"], t["first"], t["prefix"], t["depth"]))
+    for key in ("depth", "prefix", "first", "count", "is_leaf"):
+        assert np.array_equal(np.asarray(nodes[key])[got], np.asarray(t[key])[want]), key
+    check_preorder(nodes)
+
+    rng = np.random.default_rng(0)
+    rows = np.sort(rng.choice(n, 2048, replace=False))
+    rest = np.setdiff1d(np.arange(n), rows)
+    perm = np.concatenate([rows, rest])
+    ref = oracle.forces_naive_rows(x[perm], y[perm], z[perm], m[perm], 1.0, eps, 0, len(rows))
+    cpu = oracle.forces_bh_opt(x, y, z, m, 1.0, eps, theta, leaf)
+
+    def rel(acc):
+        d = np.sqrt(sum((u[rows] - v) ** 2 for u, v in zip(acc, ref)))
+        return d / np.sqrt(sum(v * v for v in ref))
+
+    g, c = rel(a), rel(cpu)
+    print(f"GPU mean {g.mean():.4g} p99 {np.quantile(g, 0.99):.4g} max {g.max():.4g}; "
+          f"CPU tree mean {c.mean():.4g} p99 {np.quantile(c, 0.99):.4g} max {c.max():.4g}")
+    assert g.mean() <= c.mean() + 2e-6
+    assert np.quantile(g, 0.99) <= 1.5 * np.quantile(c, 0.99)

@@ -9,8 +9,13 @@ CPU/tests/test2_ForceBenchmark.cpp:102-112):
                |a_gpu - a_ref| / |a_ref| <= 1e-6 for every body whose sum is
                well conditioned (S_i / |a_ref| <= 10);
                RMS over bodies of |a_gpu - a_ref| / |a_ref| <= 2e-7.
+  Hilbert-sorted mixed kernel (the default from 16,384 bodies): in addition
+               |a_gpu - a_ref| / |a_ref| <= 1e-6 for EVERY body with
+               |a_ref| > 1e-12 (the reference's own rule, no conditioning
+               clause), on the benchmark workload and the other sorted cases.
 A body whose force nearly cancels (S_i / |a_i| large) cannot be held to 1e-6
-relative by FP32 pair arithmetic; its error is bounded through S_i instead.
+relative by FP32 pair arithmetic alone; the sorted kernel evaluates its closest
+pairs (the largest terms) in FP64, which is what lets it meet the raw bound.
 """
 import numpy as np
 import pytest
@@ -34,7 +39,7 @@ def rel_errors(a, ref):
     return rel.max(), float(np.sqrt(np.mean(rel * rel)))
 
 
-def check_mixed(oracle, a, ref, state, G, eps):
+def check_mixed(oracle, a, ref, state, G, eps, raw=False):
     x, y, z, m = state[0], state[1], state[2], state[6]
     sabs = oracle.forces_abs_sum(x, y, z, m, G, eps)
     d = np.sqrt(sum((u - v) ** 2 for u, v in zip(a, ref)))
@@ -49,6 +54,8 @@ def check_mixed(oracle, a, ref, state, G, eps):
     assert info["cond_max"] <= TOL_MIXED, info
     assert rel[kappa <= KAPPA_WELL].max(initial=0.0) <= TOL_MIXED, info
     assert info["rms_rel"] <= TOL_MIXED_RMS, info
+    if raw:
+        assert info["max_rel"] <= TOL_MIXED, info
     return info
 
 
@@ -156,29 +163,35 @@ def test_mixed_sorted_near_far(nb, oracle, name):
         eps = 1e-4
     a = gpu_forces(nb, nb.DIRECT_MIXED, st, G, eps, flags=nb.MIXED_SORTED)
     ref = oracle.forces_naive(st[0], st[1], st[2], st[6], G, eps)
-    check_mixed(oracle, a, ref, st, G, eps)
+    check_mixed(oracle, a, ref, st, G, eps, raw=True)
 
 
 def test_bench_workload_forces_along_the_trajectory(nb, oracle):
     """The benchmark workload (65,536-body Plummer sphere, eps 1e-3, velocity
     Verlet dt 5e-4) run on the mixed path: the accelerations it integrates
-    with after 1, 10 and 100 steps meet the mixed tolerances against the FP64
-    direct sum of the oracle on the same positions (the sorted kernel re-sorts
-    every 8 evaluations, so these states use fresh and aged orders)."""
+    with at the start and after 1, 10, 100 and 1000 steps meet the mixed
+    tolerances against the oracle's FP64 direct sum on the same positions,
+    including the raw maximum relative error over every body (the sorted
+    kernel re-sorts every 8 evaluations, so these states use fresh and aged
+    orders)."""
     G, eps, dt = 1.0, 1e-3, 5e-4
     st = nb.plummer(65536, seed=0)
     with nb.Sim(nb.Config(method=nb.DIRECT_MIXED, G=G, softening=eps),
                 capacity=65536) as s:
         s.load(*st)
+        s.compute_forces()
         done = 0
-        for target in (1, 10, 100):
-            s.step(nb.VELOCITY_VERLET, dt, target - done)
-            done = target
+        for target in (0, 1, 10, 100, 1000):
+            if target > done:
+                s.step(nb.VELOCITY_VERLET, dt, target - done)
+                done = target
             cur = s.read_state()
             pos = (cur["x"], cur["y"], cur["z"])
             ref = oracle.forces_naive(*pos, cur["m"], G, eps)
             state = pos + (cur["vx"], cur["vy"], cur["vz"], cur["m"])
-            check_mixed(oracle, (cur["ax"], cur["ay"], cur["az"]), ref, state, G, eps)
+            info = check_mixed(oracle, (cur["ax"], cur["ay"], cur["az"]), ref, state, G, eps,
+                               raw=True)
+            print(f"step {target}: {info}")
 
 
 def test_sorted_kernel_at_2_20_bodies_sampled_rows(nb, oracle):
@@ -205,6 +218,7 @@ def test_sorted_kernel_at_2_20_bodies_sampled_rows(nb, oracle):
     assert (dd / sabs).max() <= TOL_MIXED
     well = sabs / r <= KAPPA_WELL
     assert (dd / r)[well].max() <= TOL_MIXED
+    assert (dd / r)[r > 1e-12].max() <= TOL_MIXED
     assert float(np.sqrt(np.mean((dd / r) ** 2))) <= TOL_MIXED_RMS
 
 
