@@ -103,12 +103,14 @@ typedef struct nb_config {
 #define NB_FLAG_BH_QUADRUPOLE 2
 /* NB_DIRECT_MIXED kernel choice.  By default systems of at least 16,384 bodies
  * take the Hilbert-sorted near/far kernel (far j-chunks in plain FP32 relative to
- * a warp-local origin) and smaller ones the all-pairs double-single kernel;
- * these flags force one or the other (same accuracy criteria either way).
- * Both kernels time their tile shapes and j-splits on the first evaluation of
- * each N in a process and keep the fastest; results are bit-identical within a
- * process, and between processes when the environment sets NB_AUTOTUNE=0
- * (fixed shapes), since the j-split decides the summation order. */
+ * a warp-local origin, the closest pairs in double-single) and smaller ones the
+ * all-pairs double-single kernel; these flags force one or the other.  The
+ * sorted kernel also holds every body to |da| <= 1e-6 |a| without the
+ * conditioning clause of the all-pairs kernel.  Both kernels time their CTA
+ * shapes on the first evaluation of each N in a process and keep the fastest;
+ * the j-segments and the bodies per warp (which set the summation order) are
+ * fixed by N alone, so results are bit-identical within a process and between
+ * processes on the same GPU model. */
 #define NB_FLAG_MIXED_SORTED 4
 #define NB_FLAG_MIXED_UNSORTED 8
 

@@ -59,6 +59,10 @@ namespace nb {
 namespace {
 
 constexpr int kChunk = 32;             // j-chunk = one body per lane
+constexpr int kIpt = 2;                // 32-body i-chunks per warp (fixed: it sets the bits)
+constexpr int kHitCap = 64;            // chunks with left-out pairs listed per warp
+constexpr int kExactWarps = 4;         // warps per CTA of exact_pairs_kernel
+constexpr int kExactRound = 128;       // left-out pairs evaluated per round and warp
 constexpr int kResortEvals = 8;        // force evaluations per re-sort
 constexpr bool kHilbertOrder = true;   // sort along the Hilbert curve (else Morton)
 
@@ -110,6 +114,68 @@ __global__ void split_sorted_kernel(const uint32_t *__restrict__ order,
     }
 }
 
+// A warp's box (the union of its IPT chunk boxes), its centre (the origin of
+// every staged coordinate), and the squared thresholds of its near/far and
+// left-out decisions.  Every product and sum is an explicit round-to-nearest
+// intrinsic: direct_sorted_kernel and exact_pairs_kernel must take the same
+// decisions bit for bit.
+struct WarpGeom {
+    float bmn[3], bmx[3], c[3];
+    float thr2, thr2v, thr2x;
+};
+
+template <int IPT>
+__device__ __forceinline__ WarpGeom warp_geometry(const float4 *__restrict__ box, int tile0,
+                                                  int nchunks, float far2)
+{
+    WarpGeom g;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        g.bmn[a] = 3.0e38f;
+        g.bmx[a] = -3.0e38f;
+    }
+#pragma unroll
+    for (int k = 0; k < IPT; ++k)
+        if (tile0 + k < nchunks) {
+            const float4 a = box[2 * (tile0 + k)], b = box[2 * (tile0 + k) + 1];
+            g.bmn[0] = fminf(g.bmn[0], a.x); g.bmn[1] = fminf(g.bmn[1], a.y);
+            g.bmn[2] = fminf(g.bmn[2], a.z);
+            g.bmx[0] = fmaxf(g.bmx[0], b.x); g.bmx[1] = fmaxf(g.bmx[1], b.y);
+            g.bmx[2] = fmaxf(g.bmx[2], b.z);
+        }
+    float side[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        g.c[a] = __fmul_rn(0.5f, __fadd_rn(g.bmn[a], g.bmx[a]));
+        side[a] = __fsub_rn(g.bmx[a], g.bmn[a]);
+    }
+    const float diam2 = __fmaf_rn(side[2], side[2],
+                                  __fmaf_rn(side[1], side[1], __fmul_rn(side[0], side[0])));
+    g.thr2 = __fmul_rn(far2, diam2);        // far: double-single not needed
+    g.thr2v = __fmul_rn(kVeryFar2, diam2);  // very far: Newton step not needed
+    // Pairs closer than R leave the FP32 sum and are evaluated in double-single
+    // by exact_pairs_kernel (only chunks nearer than R can hold one):
+    // R = min(kExact D, kExactSpacing s), s the mean body spacing of the warp's
+    // box, (V / 64)^(1/3) with every side padded by D / 16 so that a flat box
+    // keeps its in-plane spacing.  The spacing cap keeps sparse warps with
+    // large boxes from sending many pairs.
+    const float pad = __fmul_rn(0.0625f, sqrtf(diam2));
+    const float vol = __fmul_rn(__fmul_rn(__fadd_rn(side[0], pad), __fadd_rn(side[1], pad)),
+                                __fadd_rn(side[2], pad));
+    const float s2 = exp2f(__fmul_rn(0.6666667f, log2f(__fmul_rn(vol, 1.0f / (32.0f * IPT)))));
+    g.thr2x = fminf(__fmul_rn(kExact2, diam2), __fmul_rn(kExactSpacing2, s2));
+    return g;
+}
+
+// Squared gap between the warp's box and a j-chunk's box.
+__device__ __forceinline__ float chunk_gap2(const WarpGeom &g, float4 jmn, float4 jmx)
+{
+    const float gx = fmaxf(0.f, fmaxf(__fsub_rn(jmn.x, g.bmx[0]), __fsub_rn(g.bmn[0], jmx.x)));
+    const float gy = fmaxf(0.f, fmaxf(__fsub_rn(jmn.y, g.bmx[1]), __fsub_rn(g.bmn[1], jmx.y)));
+    const float gz = fmaxf(0.f, fmaxf(__fsub_rn(jmn.z, g.bmx[2]), __fsub_rn(g.bmn[2], jmx.z)));
+    return __fmaf_rn(gz, gz, __fmaf_rn(gy, gy, __fmul_rn(gx, gx)));
+}
+
 // One warp = 32*IPT consecutive sorted i-bodies (chunks tile0 .. tile0+IPT-1,
 // lane l of chunk k holds body (tile0 + k) * 32 + l); blockIdx.y selects the
 // j-chunks [y * seg_chunks, (y + 1) * seg_chunks).  Writes per-segment Kahan
@@ -120,7 +186,8 @@ __global__ void __launch_bounds__(WARPS * 32)
 direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                      const float4 *__restrict__ box, int n, int nchunks, float eps2,
                      int seg_chunks, float *__restrict__ psum, float *__restrict__ pcomp,
-                     float far2, double eps2d)
+                     float far2, uint32_t *__restrict__ hit_count,
+                     uint32_t *__restrict__ hit_list)
 {
     __shared__ PairTile stage[WARPS];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -128,36 +195,10 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
     if (tile0 >= nchunks) return;
     PairTile &sg = stage[w];
 
-    // the warp's box: union of its chunk boxes; centre and far threshold
-    float bmn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, bmx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
-#pragma unroll
-    for (int k = 0; k < IPT; ++k)
-        if (tile0 + k < nchunks) {
-            const float4 a = box[2 * (tile0 + k)], b = box[2 * (tile0 + k) + 1];
-            bmn[0] = fminf(bmn[0], a.x); bmn[1] = fminf(bmn[1], a.y); bmn[2] = fminf(bmn[2], a.z);
-            bmx[0] = fmaxf(bmx[0], b.x); bmx[1] = fmaxf(bmx[1], b.y); bmx[2] = fmaxf(bmx[2], b.z);
-        }
-    const float cx = 0.5f * (bmn[0] + bmx[0]), cy = 0.5f * (bmn[1] + bmx[1]),
-                cz = 0.5f * (bmn[2] + bmx[2]);
-    const float diam2 = (bmx[0] - bmn[0]) * (bmx[0] - bmn[0]) +
-                        (bmx[1] - bmn[1]) * (bmx[1] - bmn[1]) +
-                        (bmx[2] - bmn[2]) * (bmx[2] - bmn[2]);
-    const float thr2 = far2 * diam2;           // far: double-single not needed
-    const float thr2v = kVeryFar2 * diam2;     // very far: Newton step not needed
-    // Pairs closer than R leave the FP32 sum and are evaluated in double-single
-    // (only chunks nearer than R can hold one): R = min(kExact D, kExactSpacing
-    // s), s the mean body spacing of the warp's box, (V / 64)^(1/3) with every
-    // side padded by D / 16 so that a flat box keeps its in-plane spacing.  The
-    // spacing cap keeps sparse warps with large boxes from sending many pairs.
-    float thr2x;
-    {
-        const float pad = 0.0625f * sqrtf(diam2);
-        const float vol = (bmx[0] - bmn[0] + pad) * (bmx[1] - bmn[1] + pad) * (bmx[2] - bmn[2] + pad);
-        const float s2 = exp2f(0.6666667f * log2f(vol * (1.0f / (32.0f * IPT))));
-        thr2x = fminf(kExact2 * diam2, kExactSpacing2 * s2);
-    }
+    const WarpGeom gm = warp_geometry<IPT>(box, tile0, nchunks, far2);
+    const float cx = gm.c[0], cy = gm.c[1], cz = gm.c[2];
+    const float thr2 = gm.thr2, thr2v = gm.thr2v, thr2x = gm.thr2x;
     const float thrx = __fadd_rn(thr2x, eps2);
-    const DS e2ds{__double2float_rn(eps2d), __double2float_rn(eps2d - (double)__double2float_rn(eps2d))};
 
     // i-bodies relative to c, negated and duplicated into pairs
     float2 nsx[IPT], nsy[IPT], nsz[IPT], nex[IPT], ney[IPT], nez[IPT];
@@ -197,11 +238,7 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
         l = lo[jc0 * kChunk + lane];
     }
     for (int jc = jc0; jc < jc1; ++jc) {
-        const float4 jmn = box[2 * jc], jmx = box[2 * jc + 1];
-        const float gx = fmaxf(0.f, fmaxf(jmn.x - bmx[0], bmn[0] - jmx.x));
-        const float gy = fmaxf(0.f, fmaxf(jmn.y - bmx[1], bmn[1] - jmx.y));
-        const float gz = fmaxf(0.f, fmaxf(jmn.z - bmx[2], bmn[2] - jmx.z));
-        const float gap2 = gx * gx + gy * gy + gz * gz;
+        const float gap2 = chunk_gap2(gm, box[2 * jc], box[2 * jc + 1]);
         const bool far = gap2 > 0.f && gap2 >= thr2;
         const bool vfar = far && gap2 >= thr2v;
         const bool touch = !far && gap2 < thr2x;
@@ -225,7 +262,6 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
             pair_tile_put_hi(sg, lane, Sx, Sy, Sz, mj);
         else
             pair_tile_put(sg, lane, Sx, Sy, Sz, mj, Ex, Ey, Ez);
-        if (touch) pair_tile_put_mlo(sg, lane, valid ? l.w : 0.f);
         __syncwarp();
         valid = jc + 1 < jc1 && (jc + 1) * kChunk + lane < n;
         if (valid) {
@@ -259,31 +295,12 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
                     pair_term2_excl<ZERO_SOFT>(j, nsx[k], nsy[k], nsz[k], nex[k], ney[k], nez[k],
                                                e2, thrx, ax[k], ay[k], az[k], hit);
             }
-            if (__any_sync(0xffffffffu, hit)) {
-                // the same r^2 again (same operands, same bits): the lane's
-                // left-out pairs in double-single, its own body (j == i) excepted
-#pragma unroll 1
-                for (int p = 0; p < kChunk / 2; ++p) {
-                    const JPair j = pair_tile_get(sg, p);
-                    const float2 mlo = sg.g[p];
-                    const int j0 = jc * kChunk + 2 * p;
-#pragma unroll
-                    for (int k = 0; k < IPT; ++k) {
-                        const PairGeom g =
-                            pair_geom(j, nsx[k], nsy[k], nsz[k], nex[k], ney[k], nez[k], e2);
-                        const int i = (tile0 + k) * kChunk + lane;
-                        const DS xi{-nsx[k].x, -nex[k].x}, yi{-nsy[k].x, -ney[k].x},
-                            zi{-nsz[k].x, -nez[k].x};
-                        if (g.r2.x < thrx && i < n && j0 != i)
-                            pair_term_ds(DS{j.x.x, j.xl.x}, DS{j.y.x, j.yl.x}, DS{j.z.x, j.zl.x},
-                                         DS{j.m.x, mlo.x}, xi, yi, zi, e2ds, sx[k], qx[k], sy[k],
-                                         qy[k], sz[k], qz[k]);
-                        if (g.r2.y < thrx && i < n && j0 + 1 != i)
-                            pair_term_ds(DS{j.x.y, j.xl.y}, DS{j.y.y, j.yl.y}, DS{j.z.y, j.zl.y},
-                                         DS{j.m.y, mlo.y}, xi, yi, zi, e2ds, sx[k], qx[k], sy[k],
-                                         qy[k], sz[k], qz[k]);
-                    }
-                }
+            // list the chunk for exact_pairs_kernel (a chunk lies in one
+            // j-segment, so it is listed once)
+            if (__any_sync(0xffffffffu, hit) && lane == 0) {
+                const int wg = tile0 / IPT;
+                const uint32_t slot = atomicAdd(&hit_count[wg], 1u);
+                if (slot < (uint32_t)kHitCap) hit_list[(size_t)wg * kHitCap + slot] = (uint32_t)jc;
             }
         } else {
 #pragma unroll 4
@@ -323,13 +340,230 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
     }
 }
 
-// a[order[i]] = G * sum_s (sum_s - comp_s) for sorted body i: a double-single
-// sum over the segments, scaled in FP64.
+// The pairs direct_sorted_kernel left out, in double-single.  One warp per
+// warp of the main kernel (the same i-chunks and geometry); it visits the
+// chunks that warp listed (in increasing j, whatever order the segments
+// listed them in), or -- if the list overflowed -- every chunk the main kernel
+// tested for left-out pairs.  For each it stages the chunk exactly as the main
+// kernel did, recomputes the same r^2 bits, and marks the left-out pairs of
+// each lane (bit 2p + u of mk[k]: tile body 2p + u against the lane's i-body
+// k).  The marked pairs are then evaluated one per lane, whole-warp, in
+// rounds of kExactRound, and every lane adds its own bodies' terms into their
+// double-single sums in increasing j: the result does not depend on timing.
+// ex[c n + i] = the FP64 value of body i's sum (sorted order), 0 if none.
+template <int IPT>
+__global__ void __launch_bounds__(kExactWarps * 32)
+exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+                   const float4 *__restrict__ box, int n, int nchunks, float eps2, float far2,
+                   double eps2d, const uint32_t *__restrict__ hit_count,
+                   const uint32_t *__restrict__ hit_list, double *__restrict__ ex)
+{
+    __shared__ PairTile stage[kExactWarps];
+    __shared__ float ibody[kExactWarps][IPT * 32][6];        // (S, E) of x, y, z
+    __shared__ uint16_t evt[kExactWarps][kExactRound];        // (k 32 + lane) << 5 | bit
+    __shared__ float term[kExactWarps][kExactRound][6];       // (hi, lo) of x, y, z
+    __shared__ uint32_t listed[kExactWarps][kHitCap];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int wg = blockIdx.x * kExactWarps + w;
+    const int tile0 = wg * IPT;
+    if (tile0 >= nchunks) return;  // the whole warp
+    PairTile &sg = stage[w];
+    const WarpGeom gm = warp_geometry<IPT>(box, tile0, nchunks, far2);
+    const float thrx = __fadd_rn(gm.thr2x, eps2);
+    const float2 e2 = dup2(eps2);
+    const DS e2ds{__double2float_rn(eps2d),
+                  __double2float_rn(eps2d - (double)__double2float_rn(eps2d))};
+
+    float2 nsx[IPT], nsy[IPT], nsz[IPT], nex[IPT], ney[IPT], nez[IPT];
+    DS acc[IPT][3];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = (tile0 + k) * kChunk + lane;
+        float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
+        if (i < n) {
+            h = hi[i];
+            l = lo[i];
+        }
+        float S[3], E[3];
+        rel_ds(h.x, l.x, gm.c[0], S[0], E[0]);
+        rel_ds(h.y, l.y, gm.c[1], S[1], E[1]);
+        rel_ds(h.z, l.z, gm.c[2], S[2], E[2]);
+        nsx[k] = dup2(-S[0]); nex[k] = dup2(-E[0]);
+        nsy[k] = dup2(-S[1]); ney[k] = dup2(-E[1]);
+        nsz[k] = dup2(-S[2]); nez[k] = dup2(-E[2]);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            ibody[w][k * 32 + lane][2 * a] = S[a];
+            ibody[w][k * 32 + lane][2 * a + 1] = E[a];
+            acc[k][a] = DS{0.f, 0.f};
+        }
+    }
+
+    // the listed chunks in increasing order (entries are distinct)
+    const uint32_t cnt = hit_count[wg];
+    const bool use_list = cnt <= (uint32_t)kHitCap;
+    if (use_list) {
+        uint32_t v[2];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const uint32_t t = (uint32_t)(lane + 32 * r);
+            v[r] = t < cnt ? hit_list[(size_t)wg * kHitCap + t] : 0xffffffffu;
+            listed[w][t] = v[r];
+        }
+        __syncwarp();
+        int rank[2] = {0, 0};
+        for (int t = 0; t < kHitCap; ++t) {
+            const uint32_t x = listed[w][t];
+            rank[0] += x < v[0];
+            rank[1] += x < v[1];
+        }
+        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+            if ((uint32_t)(lane + 32 * r) < cnt && NB_IN_RANGE(rank[r], kHitCap))
+                listed[w][rank[r]] = v[r];
+        __syncwarp();
+    }
+
+    int next = 0, scan = 0;
+    while (true) {
+        int jc = -1;
+        if (use_list) {
+            if (next >= (int)cnt) break;
+            jc = (int)listed[w][next++];
+            if (!NB_IN_RANGE(jc, nchunks)) continue;
+        } else {
+            // every chunk the main kernel tested (not far, gap below R)
+            while (scan < nchunks) {
+                const int c = scan + lane;
+                bool t = false;
+                if (c < nchunks) {
+                    const float gap2 = chunk_gap2(gm, box[2 * c], box[2 * c + 1]);
+                    t = !(gap2 > 0.f && gap2 >= gm.thr2) && gap2 < gm.thr2x;
+                }
+                const uint32_t bal = __ballot_sync(0xffffffffu, t);
+                if (bal) {
+                    jc = scan + __ffs(bal) - 1;
+                    scan = jc + 1;
+                    break;
+                }
+                scan += 32;
+            }
+            if (jc < 0) break;
+        }
+
+        // stage the chunk as the main kernel's near path does
+        const int b = jc * kChunk + lane;
+        float Sx = 1.0e18f, Sy = 1.0e18f, Sz = 1.0e18f, Ex = 0.f, Ey = 0.f, Ez = 0.f, mj = 0.f,
+              ml = 0.f;
+        if (b < n) {
+            const float4 h = hi[b], l = lo[b];
+            rel_ds(h.x, l.x, gm.c[0], Sx, Ex);
+            rel_ds(h.y, l.y, gm.c[1], Sy, Ey);
+            rel_ds(h.z, l.z, gm.c[2], Sz, Ez);
+            mj = h.w;
+            ml = l.w;
+        }
+        __syncwarp();
+        pair_tile_put(sg, lane, Sx, Sy, Sz, mj, Ex, Ey, Ez);
+        pair_tile_put_mlo(sg, lane, ml);
+        __syncwarp();
+
+        // the left-out pairs: the main kernel's r^2 test, same operands
+        uint32_t mk[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) mk[k] = 0u;
+#pragma unroll 2
+        for (int p = 0; p < kChunk / 2; ++p) {
+            const JPair j = pair_tile_get(sg, p);
+            const int j0 = jc * kChunk + 2 * p;
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const PairGeom g = pair_geom(j, nsx[k], nsy[k], nsz[k], nex[k], ney[k], nez[k], e2);
+                const int i = (tile0 + k) * kChunk + lane;
+                const uint32_t b0 = (g.r2.x < thrx && i < n && j0 != i) ? 1u : 0u;
+                const uint32_t b1 = (g.r2.y < thrx && i < n && j0 + 1 != i) ? 2u : 0u;
+                mk[k] |= (b0 | b1) << (2 * p);
+            }
+        }
+        // event numbering: by (k, lane, bit)
+        int off[IPT], total = 0;
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            const int c = __popc(mk[k]);
+            int inc = c;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, inc, d);
+                if (lane >= d) inc += v;
+            }
+            off[k] = total + inc - c;
+            total += __shfl_sync(0xffffffffu, inc, 31);
+        }
+        for (int r = 0; r < total; r += kExactRound) {
+            const int r1 = min(total, r + kExactRound);
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                uint32_t m = mk[k];
+                for (int e = off[k]; m != 0u; ++e) {
+                    const int bit = __ffs(m) - 1;
+                    m &= m - 1u;
+                    if (e >= r && e < r1) evt[w][e - r] = (uint16_t)(((k * 32 + lane) << 5) | bit);
+                }
+            }
+            __syncwarp();
+            for (int e = lane; e < r1 - r; e += 32) {
+                const int code = evt[w][e];
+                const int il = code >> 5, bit = code & 31;
+                const int p = bit >> 1;
+                const bool u = bit & 1;
+                const float4 A = sg.s[p], B = sg.t[p], C = sg.e[p];
+                const float2 F = sg.f[p], M = sg.g[p];
+                const float *q = ibody[w][il];
+                DS t[3];
+                pair_term_ds(DS{u ? A.y : A.x, u ? C.y : C.x}, DS{u ? A.w : A.z, u ? C.w : C.z},
+                             DS{u ? B.y : B.x, u ? F.y : F.x}, DS{u ? B.w : B.z, u ? M.y : M.x},
+                             DS{q[0], q[1]}, DS{q[2], q[3]}, DS{q[4], q[5]}, e2ds, t);
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    term[w][e][2 * a] = t[a].hi;
+                    term[w][e][2 * a + 1] = t[a].lo;
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                uint32_t m = mk[k];
+                for (int e = off[k]; m != 0u; ++e) {
+                    m &= m - 1u;
+                    if (e >= r && e < r1)
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+                            acc[k][a] = ds_add(acc[k][a],
+                                               DS{term[w][e - r][2 * a], term[w][e - r][2 * a + 1]});
+                }
+            }
+            __syncwarp();
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = (tile0 + k) * kChunk + lane;
+        if (i < n)
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                ex[(size_t)a * n + i] = (double)acc[k][a].hi + (double)acc[k][a].lo;
+    }
+}
+
+// a[order[i]] = G * (sum_s (sum_s - comp_s) + ex_i) for sorted body i: a
+// double-single sum over the segments, plus the left-out pairs (ex: none when
+// NULL), scaled in FP64.
 __global__ void combine_sorted_kernel(const float *__restrict__ psum,
                                       const float *__restrict__ pcomp, int n, int segments,
                                       double G, const uint32_t *__restrict__ order,
-                                      double *__restrict__ ax, double *__restrict__ ay,
-                                      double *__restrict__ az)
+                                      const double *__restrict__ ex, double *__restrict__ ax,
+                                      double *__restrict__ ay, double *__restrict__ az)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -343,9 +577,13 @@ __global__ void combine_sorted_kernel(const float *__restrict__ psum,
     }
     const uint32_t o = order[i];
     if (!NB_IN_RANGE(o, n)) return;
-    ax[o] = G * ((double)hi[0] + (double)lo[0]);
-    ay[o] = G * ((double)hi[1] + (double)lo[1]);
-    az[o] = G * ((double)hi[2] + (double)lo[2]);
+    double a[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        a[c] = ((double)hi[c] + (double)lo[c]) + (ex ? ex[c * plane + i] : 0.0);
+    ax[o] = G * a[0];
+    ay[o] = G * a[1];
+    az[o] = G * a[2];
 }
 
 // CTA shapes the autotuner times: warps per CTA x 32-body chunks per warp.
@@ -358,7 +596,7 @@ __global__ void combine_sorted_kernel(const float *__restrict__ psum,
 struct SortedShape {
     int warps, ipt;
 };
-constexpr SortedShape kSortedShapes[] = {{4, 2}, {8, 2}, {2, 2}, {1, 2}};
+constexpr SortedShape kSortedShapes[] = {{4, kIpt}, {8, kIpt}, {2, kIpt}, {1, kIpt}};
 constexpr int kNumSortedShapes = sizeof(kSortedShapes) / sizeof(kSortedShapes[0]);
 
 template <int W, int I>
@@ -385,34 +623,41 @@ int sorted_slots_for(int warps, int ipt)
 template <int W, int I>
 void launch_sorted_shape(dim3 grid, cudaStream_t st, const float4 *hi, const float4 *lo,
                          const float4 *box, int n, double eps2, int seg_chunks, float *psum,
-                         float *pcomp)
+                         float *pcomp, uint32_t *hit_count, uint32_t *hit_list)
 {
     const int nchunks = (n + kChunk - 1) / kChunk;
     if (eps2 > 0.0)
         direct_sorted_kernel<W, I, false><<<grid, W * 32, 0, st>>>(
-            hi, lo, box, n, nchunks, (float)eps2, seg_chunks, psum, pcomp, kFarFactor2, eps2);
+            hi, lo, box, n, nchunks, (float)eps2, seg_chunks, psum, pcomp, kFarFactor2,
+            hit_count, hit_list);
     else
         direct_sorted_kernel<W, I, true><<<grid, W * 32, 0, st>>>(
-            hi, lo, box, n, nchunks, 0.0f, seg_chunks, psum, pcomp, kFarFactor2, 0.0);
+            hi, lo, box, n, nchunks, 0.0f, seg_chunks, psum, pcomp, kFarFactor2, hit_count,
+            hit_list);
 }
 
 // DirectPlan fields here: block = threads per CTA (32 * warps), ipt = chunks
 // per warp, seg_tiles = j-chunks per segment.
 bool launch_sorted(const DirectPlan &p, cudaStream_t st, const float4 *hi, const float4 *lo,
-                   const float4 *box, int n, double eps2, float *psum, float *pcomp)
+                   const float4 *box, int n, double eps2, float *psum, float *pcomp,
+                   uint32_t *hit_count, uint32_t *hit_list)
 {
     const int warps = p.block / 32;
     const int nchunks = (n + kChunk - 1) / kChunk;
     const int per_cta = warps * p.ipt;
     const dim3 grid((nchunks + per_cta - 1) / per_cta, p.segments);
     if (warps == 4 && p.ipt == 2)
-        launch_sorted_shape<4, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
+        launch_sorted_shape<4, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp,
+                                  hit_count, hit_list);
     else if (warps == 8 && p.ipt == 2)
-        launch_sorted_shape<8, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
+        launch_sorted_shape<8, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp,
+                                  hit_count, hit_list);
     else if (warps == 2 && p.ipt == 2)
-        launch_sorted_shape<2, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
+        launch_sorted_shape<2, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp,
+                                  hit_count, hit_list);
     else if (warps == 1 && p.ipt == 2)
-        launch_sorted_shape<1, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
+        launch_sorted_shape<1, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp,
+                                  hit_count, hit_list);
     else
         return false;
     return true;
@@ -445,6 +690,8 @@ void SortedBuffers::release()
     lo.release();
     partials.release();
     boxes.release();
+    hits.release();
+    exact.release();
     if (sorter) bh_destroy(sorter);
     sorter = nullptr;
     order = nullptr;
@@ -463,16 +710,42 @@ bool direct_sorted_enabled(int n, int flags)
     return on && n >= kSortedMinBodies;
 }
 
+// Warps of the main kernel (one per kIpt i-chunks) and their hit lists:
+// counts (one word per warp, zeroed before every launch) then kHitCap entries
+// per warp.
+static int sorted_warps(int n) { return ((n + kChunk - 1) / kChunk + kIpt - 1) / kIpt; }
+
 static nb_status run_sorted(const DirectPlan &p, const float4 *hi, const float4 *lo, int n,
                             double eps2, SortedBuffers &b, cudaStream_t st, float **psum_out)
 {
     NB_TRY(b.partials.reserve(sizeof(float) * 6 * (size_t)n * p.segments));
+    const size_t nw = (size_t)sorted_warps(n);
+    NB_TRY(b.hits.reserve(sizeof(uint32_t) * nw * (1 + kHitCap)));
     float *psum = b.partials.as<float>();
     float *pcomp = psum + 3 * (size_t)n * p.segments;
-    if (!launch_sorted(p, st, hi, lo, b.boxes.as<float4>(), n, eps2, psum, pcomp))
+    uint32_t *hit_count = b.hits.as<uint32_t>();
+    NB_CUDA_TRY(cudaMemsetAsync(hit_count, 0, sizeof(uint32_t) * nw, st));
+    if (!launch_sorted(p, st, hi, lo, b.boxes.as<float4>(), n, eps2, psum, pcomp, hit_count,
+                       hit_count + nw))
         return fail(NB_ERR_UNSUPPORTED, "direct_mixed_sorted: unsupported tile shape");
     NB_LAUNCH_CHECK();
     *psum_out = psum;
+    return NB_OK;
+}
+
+// The left-out pairs of the last run_sorted, into b.exact (3 n doubles).
+static nb_status run_exact_pairs(const float4 *hi, const float4 *lo, int n, double eps2,
+                                 SortedBuffers &b, cudaStream_t st, const double **ex_out)
+{
+    NB_TRY(b.exact.reserve(sizeof(double) * 3 * (size_t)n));
+    const int nw = sorted_warps(n);
+    const int nchunks = (n + kChunk - 1) / kChunk;
+    const uint32_t *hit_count = b.hits.as<uint32_t>();
+    exact_pairs_kernel<kIpt><<<(nw + kExactWarps - 1) / kExactWarps, kExactWarps * 32, 0, st>>>(
+        hi, lo, b.boxes.as<float4>(), n, nchunks, eps2 > 0.0 ? (float)eps2 : 0.0f, kFarFactor2,
+        eps2 > 0.0 ? eps2 : 0.0, hit_count, hit_count + nw, b.exact.as<double>());
+    NB_LAUNCH_CHECK();
+    *ex_out = b.exact.as<double>();
     return NB_OK;
 }
 
@@ -504,8 +777,8 @@ static nb_status autotune_sorted(const float4 *hi, const float4 *lo, int n, doub
             for (int r = 0; r < 2; ++r) {
                 NB_TRY(run_sorted(t, hi, lo, n, eps2, b, st, &psum));
                 combine_sorted_kernel<<<(n + 255) / 256, 256, 0, st>>>(
-                    psum, psum + 3 * (size_t)n * t.segments, n, t.segments, G, order, ax,
-                    ay, az);
+                    psum, psum + 3 * (size_t)n * t.segments, n, t.segments, G, order, nullptr,
+                    ax, ay, az);
                 NB_LAUNCH_CHECK();
             }
             cudaEventRecord(e1, st);
@@ -571,8 +844,10 @@ nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
     NB_TRY(run_sorted(p, hi, lo, n, eps2, b, st, &psum));
     if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
     float *pcomp = psum + 3 * (size_t)n * p.segments;
+    const double *ex = nullptr;
+    NB_TRY(run_exact_pairs(hi, lo, n, eps2, b, st, &ex));
     combine_sorted_kernel<<<(n + 255) / 256, 256, 0, st>>>(psum, pcomp, n, p.segments, G, order,
-                                                          ax, ay, az);
+                                                          ex, ax, ay, az);
     NB_LAUNCH_CHECK();
     return NB_OK;
 }

@@ -121,6 +121,8 @@ constexpr float kExactSpacing2 = 0.5625f;   // kExactSpacing = 3/4
 struct BHTree;
 struct SortedBuffers {
     DevBuf hi, lo, partials, boxes;
+    DevBuf hits;   // per warp: count of chunks with left-out pairs, then their list
+    DevBuf exact;  // the left-out pairs' sums, 3 n doubles (sorted order)
     BHTree *sorter = nullptr;
     // The sort order is a performance device only (near/far decisions use
     // the current chunk boxes, any order gives results within tolerance), so

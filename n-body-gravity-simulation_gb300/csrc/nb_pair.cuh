@@ -266,57 +266,62 @@ __device__ __forceinline__ DS ds_add(DS a, DS b)
     return quick_two_sum(s, e);
 }
 
-__device__ __forceinline__ DS ds_mul(DS a, DS b)
-{
-    const float p = __fmul_rn(a.hi, b.hi);
-    float e = __fmaf_rn(a.hi, b.hi, -p);  // exact rounding error of the product
-    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
-    return quick_two_sum(p, e);
-}
-
 // (a - b) of two normalised double-singles, exact to their ~2^-48 resolution.
 __device__ __forceinline__ DS ds_sub(DS a, DS b) { return ds_add(a, DS{-b.hi, -b.lo}); }
 
-// 1 / sqrt(x) for x > 0: the MUFU estimate y0 (~1.3e-7) and one Newton step
-// whose residual 1 - x y0^2 is formed in double-single, leaving an error of
-// order 1e-14.
-__device__ __forceinline__ DS ds_rsqrt(DS x)
+// a * b as an unevaluated sum p + e (|e| small against |p|, not normalised):
+// the FMA gives the exact error of the leading product.
+__device__ __forceinline__ DS ds_mul_loose(DS a, DS b)
 {
-    const float y0 = rsqrt_mufu(x.hi);
-    const DS y0s{y0, 0.f};
-    const DS t = ds_mul(ds_mul(x, y0s), y0s);
-    const float h = __fadd_rn(__fsub_rn(1.0f, t.hi), -t.lo);  // 1 - x y0^2, ~1e-7
-    return quick_two_sum(y0, __fmul_rn(__fmul_rn(0.5f, y0), h));
-}
-
-// (s, c) += v for a Kahan pair (value s - c) and a double-single v of any
-// magnitude: v.hi joins s through an exact two-sum (Kahan's own update
-// assumes |s| >= |v|, which a dominant term breaks), so the pair keeps about
-// 48 bits of the sum.
-__device__ __forceinline__ void kahan_add_ds(float &s, float &c, DS v)
-{
-    float S, E;
-    two_sum(s, v.hi, S, E);
-    s = S;
-    c = __fsub_rn(__fsub_rn(c, E), v.lo);
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    return DS{p, e};
 }
 
 // The pair term m_j (r_j - r_i) / (|r_j - r_i|^2 + eps2)^(3/2) in
-// double-single from the double-single coordinates (relative to a common
-// origin) and mass of both bodies; added into the Kahan pairs (sx, cx) ...
-// with kahan_add_ds.  r2 == 0 (coincident bodies, no softening) adds nothing.
+// double-single, from the double-single coordinates (relative to a common
+// origin) and masses of the two bodies; t[0..2] = x, y, z components.
+// r^2 = sum of the exact squares (FMA splits) with the low parts gathered in
+// FP32; r^-3 = y0^3 (1 + 3h/2) from the MUFU estimate y0 and its residual
+// h = 1 - r^2 y0^2 formed in double-single (h ~ 1e-7, so the dropped h^2 term
+// is ~1e-14).  About 100 FP32 operations.  r^2 == 0 (coincident bodies, no
+// softening) gives 0.
 __device__ __forceinline__ void pair_term_ds(DS xj, DS yj, DS zj, DS mj, DS xi, DS yi, DS zi,
-                                             DS eps2, float &sx, float &cx, float &sy,
-                                             float &cy, float &sz, float &cz)
+                                             DS eps2, DS t[3])
 {
     const DS dx = ds_sub(xj, xi), dy = ds_sub(yj, yi), dz = ds_sub(zj, zi);
-    const DS r2 = ds_add(ds_add(ds_mul(dx, dx), ds_mul(dy, dy)), ds_add(ds_mul(dz, dz), eps2));
-    if (!(r2.hi > 0.f)) return;
-    const DS y = ds_rsqrt(r2);
-    const DS sc = ds_mul(mj, ds_mul(ds_mul(y, y), y));
-    kahan_add_ds(sx, cx, ds_mul(sc, dx));
-    kahan_add_ds(sy, cy, ds_mul(sc, dy));
-    kahan_add_ds(sz, cz, ds_mul(sc, dz));
+    const float px = __fmul_rn(dx.hi, dx.hi), py = __fmul_rn(dy.hi, dy.hi),
+                pz = __fmul_rn(dz.hi, dz.hi);
+    const float pex = __fmaf_rn(__fadd_rn(dx.hi, dx.hi), dx.lo, __fmaf_rn(dx.hi, dx.hi, -px));
+    const float pey = __fmaf_rn(__fadd_rn(dy.hi, dy.hi), dy.lo, __fmaf_rn(dy.hi, dy.hi, -py));
+    const float pez = __fmaf_rn(__fadd_rn(dz.hi, dz.hi), dz.lo, __fmaf_rn(dz.hi, dz.hi, -pz));
+    float a, ae, b, be, c, ce;
+    two_sum(px, py, a, ae);
+    two_sum(a, pz, b, be);
+    two_sum(b, eps2.hi, c, ce);
+    const float lo = __fadd_rn(__fadd_rn(__fadd_rn(ae, be), __fadd_rn(ce, eps2.lo)),
+                               __fadd_rn(__fadd_rn(pex, pey), pez));
+    const DS r2 = quick_two_sum(c, lo);
+    if (!(r2.hi > 0.f)) {
+        t[0] = t[1] = t[2] = DS{0.f, 0.f};
+        return;
+    }
+    const float y0 = rsqrt_mufu(r2.hi);
+    const float u1 = __fmul_rn(r2.hi, y0);
+    const float u1e = __fmaf_rn(r2.lo, y0, __fmaf_rn(r2.hi, y0, -u1));
+    const float u2 = __fmul_rn(u1, y0);
+    const float u2e = __fmaf_rn(u1e, y0, __fmaf_rn(u1, y0, -u2));
+    const float h = __fsub_rn(__fsub_rn(1.0f, u2), u2e);  // 1 - r2 y0^2
+    const float q = __fmul_rn(y0, y0);
+    const float qe = __fmaf_rn(y0, y0, -q);
+    const float q3 = __fmul_rn(q, y0);
+    float q3e = __fmaf_rn(qe, y0, __fmaf_rn(q, y0, -q3));
+    q3e = __fmaf_rn(q3, __fmul_rn(1.5f, h), q3e);
+    const DS sc = ds_mul_loose(mj, DS{q3, q3e});
+    t[0] = ds_mul_loose(sc, dx);
+    t[1] = ds_mul_loose(sc, dy);
+    t[2] = ds_mul_loose(sc, dz);
 }
 
 // The plain FP32 term (coordinates already relative to a nearby origin).
