@@ -63,9 +63,10 @@ def parse():
     ap.add_argument("--bh-steps", type=int, default=20,
                     help="leapfrog steps of the Barnes-Hut N=2^20 extra (0 skips it)")
     ap.add_argument("--bh-n", type=int, default=1 << 20)
-    ap.add_argument("--bh-variants", default="rebuild,reuse4,quad",
+    ap.add_argument("--bh-variants", default="rebuild,reuse4,quad,refopen",
                     help="Barnes-Hut variants to run: rebuild every step (the configuration), "
-                         "reuse4 (tree reuse every 4 evaluations), quad (quadrupoles)")
+                         "reuse4 (tree reuse every 4 evaluations), quad (quadrupoles), refopen "
+                         "(the reference's opening rule, NB_FLAG_BH_REFERENCE_OPENING)")
     ap.add_argument("--ens-steps", type=int, default=25,
                     help="RK4 steps of the 4096-system ensemble extra (0 skips it)")
     ap.add_argument("--ens-systems", type=int, default=4096)
@@ -473,6 +474,9 @@ def run_bh(a, nb, torch, dev, stream, flush, np):
     if "quad" in variants:
         quad = timed(nb.BH_QUADRUPOLE)
         out["quadrupole"] = {k: quad[k] for k in keys}
+    if "refopen" in variants:
+        ro = timed(nb.BH_REFERENCE_OPENING)
+        out["reference_opening_rule"] = {k: ro[k] for k in keys}
     if a.bh_cpu:
         out["cpu_baseline"] = bh_cpu_baseline(state, out.get("ms_per_step"))
     return out

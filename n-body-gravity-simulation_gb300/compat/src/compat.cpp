@@ -76,6 +76,9 @@ nb_config config_of(ForceCalculator &calc)
         c.softening = std::sqrt(bh->softening_squared);
         c.theta = std::sqrt(bh->theta_sqr);
         c.leaf_capacity = bh->leaf_capacity;
+        // the reference's walks open, of every node they open, the child
+        // toward the body too (force_calculator_barnes_hut.cu:60-73)
+        c.flags |= NB_FLAG_BH_REFERENCE_OPENING;
         return c;
     }
     if (dynamic_cast<ForceCalculatorNaive *>(&calc)) {

@@ -678,12 +678,36 @@ __device__ __forceinline__ float4 monopole(const D4 &lo, const D4 &hi)
                        (float)((hi.w - lo.w) / mass), m);  // outside FP32's comfortable range
 }
 
+// The centre of a depth-d cell's parent, relative to the root centre (the
+// frame of the walk's bodies), and the cell's octant in that parent (bit 0 x,
+// bit 1 y, bit 2 z: the high side), in .w as an int; the root (d = 0), which
+// has no parent, gets 8.  The cell is read off the Morton code of any of its
+// bodies: digit k (x high) of the 3d-bit prefix halves the cube along each axis.
+__device__ __forceinline__ float4 parent_centre(uint64_t code, int d, const BHRoot *root)
+{
+    if (d == 0) return make_float4(0.f, 0.f, 0.f, __int_as_float(8));
+    const uint64_t pfx = code >> (63 - 3 * d);
+    const int dig = (int)(pfx & 7u);
+    uint32_t ix = 0, iy = 0, iz = 0;
+    for (int k = 0; k < d - 1; ++k) {
+        const int g = (int)((pfx >> (3 * (d - 1 - k))) & 7u);
+        ix = 2 * ix + ((g >> 2) & 1);
+        iy = 2 * iy + ((g >> 1) & 1);
+        iz = 2 * iz + (g & 1);
+    }
+    const double side = ldexp(root->size, -(d - 1));  // the parent's side
+    const double h = 0.5 * root->size;
+    const int oct = ((dig >> 2) & 1) | (((dig >> 1) & 1) << 1) | ((dig & 1) << 2);
+    return make_float4((float)(((double)ix + 0.5) * side - h), (float)(((double)iy + 0.5) * side - h),
+                       (float)(((double)iz + 0.5) * side - h), __int_as_float(oct));
+}
+
 __global__ void __launch_bounds__(256)
 node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__restrict__ root,
             const int *__restrict__ chain_len, const int *__restrict__ chain_depth,
             const int *__restrict__ offsets, const D4 *__restrict__ P,
             BHNode *__restrict__ nodes, unsigned char *__restrict__ node_depth,
-            BHStats *__restrict__ stats, int node_cap)
+            float4 *__restrict__ pcen, BHStats *__restrict__ stats, int node_cap)
 {
     const int i = blockIdx.x * 256 + threadIdx.x;
     if (i >= n) return;
@@ -706,6 +730,7 @@ node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__rest
         nd.size2 = root->size2[d];
         nodes[id0 + k] = nd;
         node_depth[id0 + k] = (unsigned char)d;
+        pcen[id0 + k] = parent_centre(c[i], d, root);
         leaves += leaf;
         maxd = max(maxd, d);
     }
@@ -812,13 +837,28 @@ constexpr int kWalkBlock = 128;
 // QUAD: accepted cells act as monopole + quadrupole, a = G M r / |r|^3 +
 // G (5/2 (r.Q r) r / |r|^2 - Q r) / |r|^5 with r from the body to the centre
 // of mass (softened |r| throughout).
-template <bool ZERO_SOFT, bool QUAD>
+// The reference's opening rule (NB_FLAG_BH_REFERENCE_OPENING;
+// CPU/src/force_calculator_barnes_hut_optimized.cpp and
+// CUDA/src/force_calculator_barnes_hut.cu:60-73): of every node a walk opens,
+// the child in the body's octant (relative to the node's centre) is opened
+// too, whether or not it holds the body; the opening test applies to the
+// other children.  A node is reached only after its parent was opened, so
+// the walk asks, per node, whether the body lies on the node's side of its
+// parent's centre on all three axes (pc from parent_centre).
+__device__ __forceinline__ bool toward_body(float4 pc, float x, float y, float z)
+{
+    const int oct = __float_as_int(pc.w);
+    return oct < 8 && ((x >= pc.x) == ((oct & 1) != 0)) && ((y >= pc.y) == ((oct & 2) != 0)) &&
+           ((z >= pc.z) == ((oct & 4) != 0));
+}
+
+template <bool ZERO_SOFT, bool QUAD, bool DIR>
 __global__ void __launch_bounds__(kWalkBlock)
 walk_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
             const float4 *__restrict__ body, const uint32_t *__restrict__ order, int n,
             float theta2, float eps2, double G, double *__restrict__ ax,
             double *__restrict__ ay, double *__restrict__ az, BHStats *__restrict__ stats,
-            const float4 *__restrict__ quad)
+            const float4 *__restrict__ quad, const float4 *__restrict__ pcen)
 {
     const int num_nodes = *total;
     const int lane = threadIdx.x & 31;
@@ -839,7 +879,8 @@ walk_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
         const float dz = nd.com_mass.z - p.z;
         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const bool mine = (unsigned)(i - nd.first) < (unsigned)nd.count;
-        const bool open = valid && (mine || nd.size2 >= theta2 * d2);
+        bool open = valid && (mine || nd.size2 >= theta2 * d2);
+        if (DIR) open = open || (valid && toward_body(pcen[node], p.x, p.y, p.z));
         if (__any_sync(0xffffffffu, open)) {
             if (nd.skip != node + 1) {  // internal: descend
                 ++node;
@@ -922,13 +963,13 @@ walk_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
 // load, vote and branch serve them all, and their MAC, monopole and leaf terms
 // run as f32x2 pairs.  The warp opens a node if any of its bodies does --
 // never a coarser walk than any body's own.
-template <bool ZERO_SOFT, bool QUAD, int NP>
+template <bool ZERO_SOFT, bool QUAD, int NP, bool DIR>
 __global__ void __launch_bounds__(kWalkBlock)
 walk2_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
              const float4 *__restrict__ body, const uint32_t *__restrict__ order, int n,
              float theta2, float eps2, double G, double *__restrict__ ax,
              double *__restrict__ ay, double *__restrict__ az, BHStats *__restrict__ stats,
-             const float4 *__restrict__ quad)
+             const float4 *__restrict__ quad, const float4 *__restrict__ pcen)
 {
     const int num_nodes = *total;
     constexpr int kPer = 64 * NP;  // bodies per warp
@@ -955,6 +996,7 @@ walk2_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
     int node = 0;
     while (node < num_nodes) {
         const BHNode nd = nodes[node];
+        const float4 pc = DIR ? pcen[node] : make_float4(0.f, 0.f, 0.f, 0.f);
         float2 dx[NP], dy[NP], dz[NP], d2[NP];
         bool open = false;
 #pragma unroll
@@ -969,6 +1011,9 @@ walk2_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
             const bool ob = vb[k] & (((unsigned)(ib[k] - nd.first) < (unsigned)nd.count) |
                                      (nd.size2 >= td2.y));
             open = open | oa | ob;
+            if (DIR)
+                open = open | (va[k] & toward_body(pc, -npx[k].x, -npy[k].x, -npz[k].x)) |
+                       (vb[k] & toward_body(pc, -npx[k].y, -npy[k].y, -npz[k].y));
         }
         if (__any_sync(0xffffffffu, open)) {
             if (nd.skip != node + 1) {  // internal: descend
@@ -1084,8 +1129,9 @@ struct BHTree {
     cudaEvent_t total_ready = nullptr;
     DevBuf part, root, keys0, keys1, vals0, vals1, hist, body, moments, prefix, chain_len,
         chain_depth, offsets, scan_tmp, nodes, node_depth, boxes, stats, moments2a, moments2b,
-        prefix2a, prefix2b, quad;
+        prefix2a, prefix2b, quad, pcen;
     bool with_quad = false;     // the nodes carry quadrupoles (quad, 2 float4 per node)
+    bool ref_open = false;      // the reference's opening rule (the child toward the body too)
     const uint64_t *sorted_codes = nullptr;
     const uint32_t *order = nullptr;
     bool tree_valid = false;    // nodes/order describe a build of these bodies' count
@@ -1111,7 +1157,7 @@ void bh_destroy(BHTree *t)
                       &t->hist, &t->body, &t->moments, &t->prefix, &t->chain_len,
                       &t->chain_depth, &t->offsets, &t->scan_tmp, &t->nodes, &t->node_depth,
                       &t->boxes, &t->stats, &t->moments2a, &t->moments2b, &t->prefix2a,
-                      &t->prefix2b, &t->quad};
+                      &t->prefix2b, &t->quad, &t->pcen};
     for (DevBuf *b : bufs) b->release();
     if (t->h_total) cudaFreeHost(t->h_total);
     if (t->total_ready) cudaEventDestroy(t->total_ready);
@@ -1273,23 +1319,32 @@ int walk_pairs()
     return np;
 }
 
-template <bool ZS, bool Q>
+template <bool ZS, bool Q, bool D>
 void walk_launch(BHTree *t, int n, float theta2, float eps2, double G, double *ax, double *ay,
                  double *az, cudaStream_t st)
 {
     const int np = walk_pairs();
+    const float4 *pc = t->pcen.as<float4>();
     if (np == 2)
-        walk2_kernel<ZS, Q, 2><<<div_up(n, 4 * kWalkBlock), kWalkBlock, 0, st>>>(
+        walk2_kernel<ZS, Q, 2, D><<<div_up(n, 4 * kWalkBlock), kWalkBlock, 0, st>>>(
             t->nodes.as<BHNode>(), d_total(t), t->body.as<float4>(), t->order, n, theta2,
-            eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>());
+            eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>(), pc);
     else if (np == 1)
-        walk2_kernel<ZS, Q, 1><<<div_up(n, 2 * kWalkBlock), kWalkBlock, 0, st>>>(
+        walk2_kernel<ZS, Q, 1, D><<<div_up(n, 2 * kWalkBlock), kWalkBlock, 0, st>>>(
             t->nodes.as<BHNode>(), d_total(t), t->body.as<float4>(), t->order, n, theta2,
-            eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>());
+            eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>(), pc);
     else
-        walk_kernel<ZS, Q><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
+        walk_kernel<ZS, Q, D><<<div_up(n, kWalkBlock), kWalkBlock, 0, st>>>(
             t->nodes.as<BHNode>(), d_total(t), t->body.as<float4>(), t->order, n, theta2,
-            eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>());
+            eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>(), pc);
+}
+
+template <bool ZS, bool Q>
+void walk_launch_rule(BHTree *t, int n, float theta2, float eps2, double G, double *ax,
+                      double *ay, double *az, cudaStream_t st)
+{
+    if (t->ref_open) walk_launch<ZS, Q, true>(t, n, theta2, eps2, G, ax, ay, az, st);
+    else walk_launch<ZS, Q, false>(t, n, theta2, eps2, G, ax, ay, az, st);
 }
 
 static nb_status launch_walk(BHTree *t, int n, double G, double eps2, double theta, double *ax,
@@ -1299,11 +1354,11 @@ static nb_status launch_walk(BHTree *t, int n, double G, double eps2, double the
     const float th2 = (float)(theta * theta), e2 = (float)eps2;
     if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
     if (t->with_quad) {
-        if (eps2 > 0.0) walk_launch<false, true>(t, n, th2, e2, G, ax, ay, az, st);
-        else walk_launch<true, true>(t, n, th2, 0.0f, G, ax, ay, az, st);
+        if (eps2 > 0.0) walk_launch_rule<false, true>(t, n, th2, e2, G, ax, ay, az, st);
+        else walk_launch_rule<true, true>(t, n, th2, 0.0f, G, ax, ay, az, st);
     } else {
-        if (eps2 > 0.0) walk_launch<false, false>(t, n, th2, e2, G, ax, ay, az, st);
-        else walk_launch<true, false>(t, n, th2, 0.0f, G, ax, ay, az, st);
+        if (eps2 > 0.0) walk_launch_rule<false, false>(t, n, th2, e2, G, ax, ay, az, st);
+        else walk_launch_rule<true, false>(t, n, th2, 0.0f, G, ax, ay, az, st);
     }
     NB_LAUNCH_CHECK();
     if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
@@ -1367,10 +1422,11 @@ static nb_status refit(BHTree *t, const double *x, const double *y, const double
 nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *z,
                      const double *m, int n, double G, double eps2, double theta,
                      int leaf_capacity, double *ax, double *ay, double *az, cudaStream_t st,
-                     const KernelTimer *timer, int reuse, bool quad)
+                     const KernelTimer *timer, int reuse, bool quad, bool ref_open)
 {
     if (n <= 0) return NB_OK;
     t->with_quad = quad;
+    t->ref_open = ref_open;
     if (ax && reuse > 1 && t->tree_valid && t->n == n && t->evals_since_build < reuse) {
         NB_TRY(refit(t, x, y, z, m, n, st));
         if (quad) NB_TRY(compute_quads(t, x, y, z, m, n, st));
@@ -1412,6 +1468,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     const size_t cap = node_bound(n, leaf_capacity);
     NB_TRY(t->nodes.reserve(sizeof(BHNode) * cap));
     NB_TRY(t->node_depth.reserve(cap));
+    NB_TRY(t->pcen.reserve(sizeof(float4) * cap));
     if (!t->h_total) NB_CUDA_TRY(cudaMallocHost(&t->h_total, sizeof(int)));
     if (!t->total_ready) NB_CUDA_TRY(cudaEventCreateWithFlags(&t->total_ready,
                                                               cudaEventDisableTiming));
@@ -1433,8 +1490,8 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
                                                 t->chain_len.as<int>(), t->chain_depth.as<int>(),
                                                 t->offsets.as<int>(), t->prefix.as<D4>(),
                                                 t->nodes.as<BHNode>(),
-                                                t->node_depth.as<unsigned char>(), stats,
-                                                t->node_cap);
+                                                t->node_depth.as<unsigned char>(),
+                                                t->pcen.as<float4>(), stats, t->node_cap);
     NB_LAUNCH_CHECK();
     if (quad) NB_TRY(compute_quads(t, x, y, z, m, n, st));
     t->tree_valid = true;

@@ -60,9 +60,8 @@ namespace {
 
 constexpr int kChunk = 32;             // j-chunk = one body per lane
 constexpr int kIpt = 2;                // 32-body i-chunks per warp (fixed: it sets the bits)
-constexpr int kHitCap = 64;            // chunks with left-out pairs listed per warp
-constexpr int kExactWarps = 4;         // warps per CTA of exact_pairs_kernel
-constexpr int kExactRound = 128;       // left-out pairs evaluated per round and warp
+constexpr int kExactWarps = 8;         // warps of exact_pairs_kernel per main-kernel warp
+constexpr int kExactRound = 64;        // left-out pairs evaluated per round and warp
 constexpr int kResortEvals = 8;        // force evaluations per re-sort
 constexpr bool kHilbertOrder = true;   // sort along the Hilbert curve (else Morton)
 
@@ -186,8 +185,7 @@ __global__ void __launch_bounds__(WARPS * 32)
 direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                      const float4 *__restrict__ box, int n, int nchunks, float eps2,
                      int seg_chunks, float *__restrict__ psum, float *__restrict__ pcomp,
-                     float far2, uint32_t *__restrict__ hit_count,
-                     uint32_t *__restrict__ hit_list)
+                     float far2)
 {
     __shared__ PairTile stage[WARPS];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -286,6 +284,7 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
                     pair_term2_far<true>(j, nsx[k], nsy[k], nsz[k], e2, ax[k], ay[k], az[k]);
             }
         } else if (touch) {
+            // pairs closer than R are left to exact_pairs_kernel
             bool hit = false;
 #pragma unroll 4
             for (int p = 0; p < kChunk / 2; ++p) {
@@ -294,13 +293,6 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
                 for (int k = 0; k < IPT; ++k)
                     pair_term2_excl<ZERO_SOFT>(j, nsx[k], nsy[k], nsz[k], nex[k], ney[k], nez[k],
                                                e2, thrx, ax[k], ay[k], az[k], hit);
-            }
-            // list the chunk for exact_pairs_kernel (a chunk lies in one
-            // j-segment, so it is listed once)
-            if (__any_sync(0xffffffffu, hit) && lane == 0) {
-                const int wg = tile0 / IPT;
-                const uint32_t slot = atomicAdd(&hit_count[wg], 1u);
-                if (slot < (uint32_t)kHitCap) hit_list[(size_t)wg * kHitCap + slot] = (uint32_t)jc;
             }
         } else {
 #pragma unroll 4
@@ -340,33 +332,35 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
     }
 }
 
-// The pairs direct_sorted_kernel left out, in double-single.  One warp per
-// warp of the main kernel (the same i-chunks and geometry); it visits the
-// chunks that warp listed (in increasing j, whatever order the segments
-// listed them in), or -- if the list overflowed -- every chunk the main kernel
-// tested for left-out pairs.  For each it stages the chunk exactly as the main
-// kernel did, recomputes the same r^2 bits, and marks the left-out pairs of
-// each lane (bit 2p + u of mk[k]: tile body 2p + u against the lane's i-body
-// k).  The marked pairs are then evaluated one per lane, whole-warp, in
-// rounds of kExactRound, and every lane adds its own bodies' terms into their
-// double-single sums in increasing j: the result does not depend on timing.
+// The pairs direct_sorted_kernel leaves out, in double-single.  It needs
+// nothing from that kernel -- it takes the same decisions from the same data
+// -- so it runs beside it on a second stream.  One CTA per warp of the main
+// kernel (the same i-chunks and geometry) and kExactWarps warps in it: warp w
+// takes the chunks jc = w (mod kExactWarps) that the main kernel tests for
+// left-out pairs (not far, nearer than R), in increasing order, skipping those
+// that no lane's i-body comes within R of.  For each it stages the chunk
+// exactly as the main kernel does, recomputes the same r^2 bits, and marks the
+// left-out pairs of each lane (bit 2p + u of mk[k]: tile body 2p + u against
+// the lane's i-body k).  The marked pairs are evaluated one per lane,
+// whole-warp, in rounds of kExactRound, and every lane adds its own bodies'
+// terms into their double-single sums in increasing j; the warps' sums are
+// then added in warp order.  The result does not depend on timing.
 // ex[c n + i] = the FP64 value of body i's sum (sorted order), 0 if none.
 template <int IPT>
 __global__ void __launch_bounds__(kExactWarps * 32)
 exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                    const float4 *__restrict__ box, int n, int nchunks, float eps2, float far2,
-                   double eps2d, const uint32_t *__restrict__ hit_count,
-                   const uint32_t *__restrict__ hit_list, double *__restrict__ ex)
+                   double eps2d, double *__restrict__ ex)
 {
     __shared__ PairTile stage[kExactWarps];
-    __shared__ float ibody[kExactWarps][IPT * 32][6];        // (S, E) of x, y, z
+    __shared__ float ibody[IPT * 32][6];                      // (S, E) of x, y, z
     __shared__ uint16_t evt[kExactWarps][kExactRound];        // (k 32 + lane) << 5 | bit
     __shared__ float term[kExactWarps][kExactRound][6];       // (hi, lo) of x, y, z
-    __shared__ uint32_t listed[kExactWarps][kHitCap];
+    __shared__ float red[kExactWarps][IPT * 32][6];           // the warps' sums
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int wg = blockIdx.x * kExactWarps + w;
+    const int wg = blockIdx.x;
     const int tile0 = wg * IPT;
-    if (tile0 >= nchunks) return;  // the whole warp
+    if (tile0 >= nchunks) return;  // the whole CTA
     PairTile &sg = stage[w];
     const WarpGeom gm = warp_geometry<IPT>(box, tile0, nchunks, far2);
     const float thrx = __fadd_rn(gm.thr2x, eps2);
@@ -393,64 +387,80 @@ exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
         nsz[k] = dup2(-S[2]); nez[k] = dup2(-E[2]);
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            ibody[w][k * 32 + lane][2 * a] = S[a];
-            ibody[w][k * 32 + lane][2 * a + 1] = E[a];
+            if (w == 0) {
+                ibody[k * 32 + lane][2 * a] = S[a];
+                ibody[k * 32 + lane][2 * a + 1] = E[a];
+            }
             acc[k][a] = DS{0.f, 0.f};
         }
     }
+    __syncthreads();
 
-    // the listed chunks in increasing order (entries are distinct)
-    const uint32_t cnt = hit_count[wg];
-    const bool use_list = cnt <= (uint32_t)kHitCap;
-    if (use_list) {
-        uint32_t v[2];
+    // the lane's i-bodies' box, for the per-lane test of a chunk
+    float lmn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, lmx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
 #pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const uint32_t t = (uint32_t)(lane + 32 * r);
-            v[r] = t < cnt ? hit_list[(size_t)wg * kHitCap + t] : 0xffffffffu;
-            listed[w][t] = v[r];
-        }
-        __syncwarp();
-        int rank[2] = {0, 0};
-        for (int t = 0; t < kHitCap; ++t) {
-            const uint32_t x = listed[w][t];
-            rank[0] += x < v[0];
-            rank[1] += x < v[1];
-        }
-        __syncwarp();
+    for (int k = 0; k < IPT; ++k)
+        if ((tile0 + k) * kChunk + lane < n) {
+            const float q[3] = {-nsx[k].x, -nsy[k].x, -nsz[k].x};
 #pragma unroll
-        for (int r = 0; r < 2; ++r)
-            if ((uint32_t)(lane + 32 * r) < cnt && NB_IN_RANGE(rank[r], kHitCap))
-                listed[w][rank[r]] = v[r];
-        __syncwarp();
-    }
+            for (int a = 0; a < 3; ++a) {
+                lmn[a] = fminf(lmn[a], q[a]);
+                lmx[a] = fmaxf(lmx[a], q[a]);
+            }
+        }
+    // The test below only skips work, so it must never skip a chunk that holds
+    // a left-out pair: R grows by a slack far above the FP32 roundings that
+    // separate the boxes (hi coordinates) from the staged ones and the box
+    // distance from the pair's r^2 (softening included).
+    const float Rw = sqrtf(gm.thr2x);
+    const float cmag = fmaxf(fabsf(gm.c[0]), fmaxf(fabsf(gm.c[1]), fabsf(gm.c[2])));
+    const float e2slack = 1e-6f * (gm.thr2x + eps2);
 
-    int next = 0, scan = 0;
+    int scan = w;
     while (true) {
+        // the next chunk jc = w (mod kExactWarps) the main kernel tests, with
+        // a lane whose bodies come within R of its box
         int jc = -1;
-        if (use_list) {
-            if (next >= (int)cnt) break;
-            jc = (int)listed[w][next++];
-            if (!NB_IN_RANGE(jc, nchunks)) continue;
-        } else {
-            // every chunk the main kernel tested (not far, gap below R)
-            while (scan < nchunks) {
-                const int c = scan + lane;
-                bool t = false;
-                if (c < nchunks) {
-                    const float gap2 = chunk_gap2(gm, box[2 * c], box[2 * c + 1]);
-                    t = !(gap2 > 0.f && gap2 >= gm.thr2) && gap2 < gm.thr2x;
-                }
-                const uint32_t bal = __ballot_sync(0xffffffffu, t);
-                if (bal) {
-                    jc = scan + __ffs(bal) - 1;
-                    scan = jc + 1;
+        while (scan < nchunks) {
+            const int c = scan + kExactWarps * lane;
+            bool t = false;
+            float4 jmn = make_float4(0.f, 0.f, 0.f, 0.f), jmx = jmn;
+            if (c < nchunks) {
+                jmn = box[2 * c];
+                jmx = box[2 * c + 1];
+                const float gap2 = chunk_gap2(gm, jmn, jmx);
+                t = !(gap2 > 0.f && gap2 >= gm.thr2) && gap2 < gm.thr2x;
+            }
+            uint32_t cand = __ballot_sync(0xffffffffu, t);
+            while (cand) {
+                const int src = __ffs(cand) - 1;
+                cand &= cand - 1u;
+                // this lane's bodies against the candidate's box (relative to c)
+                const float bx0 = __shfl_sync(0xffffffffu, jmn.x, src) - gm.c[0];
+                const float by0 = __shfl_sync(0xffffffffu, jmn.y, src) - gm.c[1];
+                const float bz0 = __shfl_sync(0xffffffffu, jmn.z, src) - gm.c[2];
+                const float bx1 = __shfl_sync(0xffffffffu, jmx.x, src) - gm.c[0];
+                const float by1 = __shfl_sync(0xffffffffu, jmx.y, src) - gm.c[1];
+                const float bz1 = __shfl_sync(0xffffffffu, jmx.z, src) - gm.c[2];
+                const float gx = fmaxf(0.f, fmaxf(bx0 - lmx[0], lmn[0] - bx1));
+                const float gy = fmaxf(0.f, fmaxf(by0 - lmx[1], lmn[1] - by1));
+                const float gz = fmaxf(0.f, fmaxf(bz0 - lmx[2], lmn[2] - bz1));
+                const float mag = cmag + fmaxf(fmaxf(fabsf(bx0), fabsf(bx1)),
+                                               fmaxf(fmaxf(fabsf(by0), fabsf(by1)),
+                                                     fmaxf(fabsf(bz0), fabsf(bz1))));
+                const float Re = Rw + 1e-6f * mag;
+                if (__any_sync(0xffffffffu, gx * gx + gy * gy + gz * gz <= Re * Re + e2slack)) {
+                    jc = scan + kExactWarps * src;
                     break;
                 }
-                scan += 32;
             }
-            if (jc < 0) break;
+            if (jc >= 0) {
+                scan = jc + kExactWarps;
+                break;
+            }
+            scan += 32 * kExactWarps;
         }
+        if (jc < 0) break;
 
         // stage the chunk as the main kernel's near path does
         const int b = jc * kChunk + lane;
@@ -486,7 +496,7 @@ exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                 mk[k] |= (b0 | b1) << (2 * p);
             }
         }
-        // event numbering: by (k, lane, bit)
+        // pairs numbered by (k, lane, bit)
         int off[IPT], total = 0;
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
@@ -519,7 +529,7 @@ exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                 const bool u = bit & 1;
                 const float4 A = sg.s[p], B = sg.t[p], C = sg.e[p];
                 const float2 F = sg.f[p], M = sg.g[p];
-                const float *q = ibody[w][il];
+                const float *q = ibody[il];
                 DS t[3];
                 pair_term_ds(DS{u ? A.y : A.x, u ? C.y : C.x}, DS{u ? A.w : A.z, u ? C.w : C.z},
                              DS{u ? B.y : B.x, u ? F.y : F.x}, DS{u ? B.w : B.z, u ? M.y : M.x},
@@ -546,13 +556,30 @@ exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
             __syncwarp();
         }
     }
+
+    // the warps' sums in warp order
+#pragma unroll
+    for (int k = 0; k < IPT; ++k)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            red[w][k * 32 + lane][2 * a] = acc[k][a].hi;
+            red[w][k * 32 + lane][2 * a + 1] = acc[k][a].lo;
+        }
+    __syncthreads();
+    if (w != 0) return;
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
         const int i = (tile0 + k) * kChunk + lane;
+        DS sum[3] = {DS{0.f, 0.f}, DS{0.f, 0.f}, DS{0.f, 0.f}};
+        for (int v = 0; v < kExactWarps; ++v)
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                sum[a] = ds_add(sum[a], DS{red[v][k * 32 + lane][2 * a],
+                                           red[v][k * 32 + lane][2 * a + 1]});
         if (i < n)
 #pragma unroll
             for (int a = 0; a < 3; ++a)
-                ex[(size_t)a * n + i] = (double)acc[k][a].hi + (double)acc[k][a].lo;
+                ex[(size_t)a * n + i] = (double)sum[a].hi + (double)sum[a].lo;
     }
 }
 
@@ -623,41 +650,34 @@ int sorted_slots_for(int warps, int ipt)
 template <int W, int I>
 void launch_sorted_shape(dim3 grid, cudaStream_t st, const float4 *hi, const float4 *lo,
                          const float4 *box, int n, double eps2, int seg_chunks, float *psum,
-                         float *pcomp, uint32_t *hit_count, uint32_t *hit_list)
+                         float *pcomp)
 {
     const int nchunks = (n + kChunk - 1) / kChunk;
     if (eps2 > 0.0)
         direct_sorted_kernel<W, I, false><<<grid, W * 32, 0, st>>>(
-            hi, lo, box, n, nchunks, (float)eps2, seg_chunks, psum, pcomp, kFarFactor2,
-            hit_count, hit_list);
+            hi, lo, box, n, nchunks, (float)eps2, seg_chunks, psum, pcomp, kFarFactor2);
     else
         direct_sorted_kernel<W, I, true><<<grid, W * 32, 0, st>>>(
-            hi, lo, box, n, nchunks, 0.0f, seg_chunks, psum, pcomp, kFarFactor2, hit_count,
-            hit_list);
+            hi, lo, box, n, nchunks, 0.0f, seg_chunks, psum, pcomp, kFarFactor2);
 }
 
 // DirectPlan fields here: block = threads per CTA (32 * warps), ipt = chunks
 // per warp, seg_tiles = j-chunks per segment.
 bool launch_sorted(const DirectPlan &p, cudaStream_t st, const float4 *hi, const float4 *lo,
-                   const float4 *box, int n, double eps2, float *psum, float *pcomp,
-                   uint32_t *hit_count, uint32_t *hit_list)
+                   const float4 *box, int n, double eps2, float *psum, float *pcomp)
 {
     const int warps = p.block / 32;
     const int nchunks = (n + kChunk - 1) / kChunk;
     const int per_cta = warps * p.ipt;
     const dim3 grid((nchunks + per_cta - 1) / per_cta, p.segments);
     if (warps == 4 && p.ipt == 2)
-        launch_sorted_shape<4, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp,
-                                  hit_count, hit_list);
+        launch_sorted_shape<4, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
     else if (warps == 8 && p.ipt == 2)
-        launch_sorted_shape<8, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp,
-                                  hit_count, hit_list);
+        launch_sorted_shape<8, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
     else if (warps == 2 && p.ipt == 2)
-        launch_sorted_shape<2, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp,
-                                  hit_count, hit_list);
+        launch_sorted_shape<2, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
     else if (warps == 1 && p.ipt == 2)
-        launch_sorted_shape<1, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp,
-                                  hit_count, hit_list);
+        launch_sorted_shape<1, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
     else
         return false;
     return true;
@@ -690,8 +710,12 @@ void SortedBuffers::release()
     lo.release();
     partials.release();
     boxes.release();
-    hits.release();
     exact.release();
+    if (side) cudaStreamDestroy(side);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    side = nullptr;
+    fork = join = nullptr;
     if (sorter) bh_destroy(sorter);
     sorter = nullptr;
     order = nullptr;
@@ -710,42 +734,45 @@ bool direct_sorted_enabled(int n, int flags)
     return on && n >= kSortedMinBodies;
 }
 
-// Warps of the main kernel (one per kIpt i-chunks) and their hit lists:
-// counts (one word per warp, zeroed before every launch) then kHitCap entries
-// per warp.
+// Warps of the main kernel (one per kIpt i-chunks).
 static int sorted_warps(int n) { return ((n + kChunk - 1) / kChunk + kIpt - 1) / kIpt; }
 
 static nb_status run_sorted(const DirectPlan &p, const float4 *hi, const float4 *lo, int n,
                             double eps2, SortedBuffers &b, cudaStream_t st, float **psum_out)
 {
     NB_TRY(b.partials.reserve(sizeof(float) * 6 * (size_t)n * p.segments));
-    const size_t nw = (size_t)sorted_warps(n);
-    NB_TRY(b.hits.reserve(sizeof(uint32_t) * nw * (1 + kHitCap)));
     float *psum = b.partials.as<float>();
     float *pcomp = psum + 3 * (size_t)n * p.segments;
-    uint32_t *hit_count = b.hits.as<uint32_t>();
-    NB_CUDA_TRY(cudaMemsetAsync(hit_count, 0, sizeof(uint32_t) * nw, st));
-    if (!launch_sorted(p, st, hi, lo, b.boxes.as<float4>(), n, eps2, psum, pcomp, hit_count,
-                       hit_count + nw))
+    if (!launch_sorted(p, st, hi, lo, b.boxes.as<float4>(), n, eps2, psum, pcomp))
         return fail(NB_ERR_UNSUPPORTED, "direct_mixed_sorted: unsupported tile shape");
     NB_LAUNCH_CHECK();
     *psum_out = psum;
     return NB_OK;
 }
 
-// The left-out pairs of the last run_sorted, into b.exact (3 n doubles).
-static nb_status run_exact_pairs(const float4 *hi, const float4 *lo, int n, double eps2,
-                                 SortedBuffers &b, cudaStream_t st, const double **ex_out)
+// The left-out pairs, into b.exact (3 n doubles), on b.side: the kernel
+// waits for the staging on st (fork) and st waits for it before the combine
+// (join).  The side stream has the highest priority, so the exact CTAs start
+// at once and their longest chains run while the main kernel fills the GPU.
+static nb_status launch_exact_pairs(const float4 *hi, const float4 *lo, int n, double eps2,
+                                    SortedBuffers &b, cudaStream_t st)
 {
     NB_TRY(b.exact.reserve(sizeof(double) * 3 * (size_t)n));
-    const int nw = sorted_warps(n);
+    if (!b.side) {
+        int least = 0, greatest = 0;
+        NB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        NB_CUDA_TRY(cudaStreamCreateWithPriority(&b.side, cudaStreamNonBlocking, greatest));
+        NB_CUDA_TRY(cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming));
+        NB_CUDA_TRY(cudaEventCreateWithFlags(&b.join, cudaEventDisableTiming));
+    }
+    NB_CUDA_TRY(cudaEventRecord(b.fork, st));
+    NB_CUDA_TRY(cudaStreamWaitEvent(b.side, b.fork, 0));
     const int nchunks = (n + kChunk - 1) / kChunk;
-    const uint32_t *hit_count = b.hits.as<uint32_t>();
-    exact_pairs_kernel<kIpt><<<(nw + kExactWarps - 1) / kExactWarps, kExactWarps * 32, 0, st>>>(
+    exact_pairs_kernel<kIpt><<<sorted_warps(n), kExactWarps * 32, 0, b.side>>>(
         hi, lo, b.boxes.as<float4>(), n, nchunks, eps2 > 0.0 ? (float)eps2 : 0.0f, kFarFactor2,
-        eps2 > 0.0 ? eps2 : 0.0, hit_count, hit_count + nw, b.exact.as<double>());
+        eps2 > 0.0 ? eps2 : 0.0, b.exact.as<double>());
     NB_LAUNCH_CHECK();
-    *ex_out = b.exact.as<double>();
+    NB_CUDA_TRY(cudaEventRecord(b.join, b.side));
     return NB_OK;
 }
 
@@ -839,15 +866,15 @@ nb_status direct_mixed_sorted(const double *x, const double *y, const double *z,
             NB_TRY(autotune_sorted(hi, lo, n, eps2, G, order, ax, ay, az, b, st, &p));
         else p = sorted_plan_for_shape(n, 1, 2);
     }
+    NB_TRY(launch_exact_pairs(hi, lo, n, eps2, b, st));
     if (timer && timer->start) NB_CUDA_TRY(cudaEventRecord(timer->start, st));
     float *psum = nullptr;
     NB_TRY(run_sorted(p, hi, lo, n, eps2, b, st, &psum));
     if (timer && timer->stop) NB_CUDA_TRY(cudaEventRecord(timer->stop, st));
     float *pcomp = psum + 3 * (size_t)n * p.segments;
-    const double *ex = nullptr;
-    NB_TRY(run_exact_pairs(hi, lo, n, eps2, b, st, &ex));
+    NB_CUDA_TRY(cudaStreamWaitEvent(st, b.join, 0));
     combine_sorted_kernel<<<(n + 255) / 256, 256, 0, st>>>(psum, pcomp, n, p.segments, G, order,
-                                                          ex, ax, ay, az);
+                                                          b.exact.as<double>(), ax, ay, az);
     NB_LAUNCH_CHECK();
     return NB_OK;
 }

@@ -121,8 +121,9 @@ constexpr float kExactSpacing2 = 0.5625f;   // kExactSpacing = 3/4
 struct BHTree;
 struct SortedBuffers {
     DevBuf hi, lo, partials, boxes;
-    DevBuf hits;   // per warp: count of chunks with left-out pairs, then their list
     DevBuf exact;  // the left-out pairs' sums, 3 n doubles (sorted order)
+    cudaStream_t side = nullptr;              // the exact-pair kernel's stream
+    cudaEvent_t fork = nullptr, join = nullptr;
     BHTree *sorter = nullptr;
     // The sort order is a performance device only (near/far decisions use
     // the current chunk boxes, any order gives results within tolerance), so
@@ -257,11 +258,13 @@ void bh_destroy(BHTree *t);
 // G * acceleration (FP64) in the original body order.  reuse > 1: the tree is
 // rebuilt every `reuse` walks; the walks in between keep its topology and
 // refit monopoles and cell sides to the current positions.  quad: accepted
-// cells act with their quadrupole moments too.
+// cells act with their quadrupole moments too.  ref_open: the walk also opens,
+// of every node it opens, the child toward the body (the reference's rule).
 nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *z,
                      const double *m, int n, double G, double eps2, double theta,
                      int leaf_capacity, double *ax, double *ay, double *az, cudaStream_t st,
-                     const KernelTimer *timer = nullptr, int reuse = 1, bool quad = false);
+                     const KernelTimer *timer = nullptr, int reuse = 1, bool quad = false,
+                     bool ref_open = false);
 // The next bh_compute rebuilds (the bodies were replaced).
 void bh_invalidate(BHTree *t);
 // A replayed build changed the node count behind the host's back.

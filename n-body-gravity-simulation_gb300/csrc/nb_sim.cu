@@ -145,7 +145,8 @@ nb_status eval_forces(nb_sim *s, const double *px, const double *py, const doubl
         return bh_compute(s->bh, px, py, pz, s->m(), n, s->cfg.G, eps2, s->cfg.theta,
                           s->cfg.leaf_capacity, oax, oay, oaz, s->stream, timer,
                           NB_FLAG_BH_REUSE_OF(s->cfg.flags),
-                          (s->cfg.flags & NB_FLAG_BH_QUADRUPOLE) != 0);
+                          (s->cfg.flags & NB_FLAG_BH_QUADRUPOLE) != 0,
+                          (s->cfg.flags & NB_FLAG_BH_REFERENCE_OPENING) != 0);
     default:
         return fail(NB_ERR_INVALID_ARGUMENT, "unknown force method");
     }

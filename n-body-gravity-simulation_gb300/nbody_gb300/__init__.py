@@ -122,6 +122,7 @@ def kernel_launch_count() -> int:
 
 
 BH_QUADRUPOLE = 2  # NB_FLAG_BH_QUADRUPOLE
+BH_REFERENCE_OPENING = 16  # NB_FLAG_BH_REFERENCE_OPENING: the reference's opening rule
 MIXED_SORTED = 4  # NB_FLAG_MIXED_SORTED: force the Hilbert-sorted near/far kernel
 MIXED_UNSORTED = 8  # NB_FLAG_MIXED_UNSORTED: force the all-pairs double-single kernel
 

@@ -14,9 +14,10 @@ Within tolerance (floating point):
   - forces vs the FP64 direct sum inside the reference's own Barnes-Hut
     accuracy envelope at theta = 0.5 (CUDA/outputs/output1_2.txt and
     CPU/outputs/output2_4.txt: mean relative error 2.8e-3 at N = 10,000);
-    the warp-cooperative walk opens every node any body of the warp opens, so
-    it must be at least as accurate as the CPU node-pool tree on the same
-    input.
+    the walk follows the reference's opening rule (an opened node's child
+    toward the body is opened too) and opens every node any body of the warp
+    opens, so it must be at least as accurate as the CPU node-pool tree on the
+    same input.
 """
 import json
 import os
@@ -36,10 +37,10 @@ def cube(oracle, n, seed=42, order=1):
     return x, y, z, zero, zero.copy(), zero.copy(), m
 
 
-def bh_sim(nb, state, G=1.0, eps=0.0, theta=0.5, leaf=8):
+def bh_sim(nb, state, G=1.0, eps=0.0, theta=0.5, leaf=8, flags=0):
     n = len(state[0])
     s = nb.Sim(nb.Config(method=nb.BARNES_HUT, G=G, softening=eps, theta=theta,
-                         leaf_capacity=leaf), capacity=n)
+                         leaf_capacity=leaf, flags=flags), capacity=n)
     s.load(*state)
     return s
 
@@ -180,6 +181,30 @@ def test_force_accuracy_plummer(nb, oracle, theta):
     cavg, cmx = _errors(cpu_bh, ref)
     assert avg <= 1.05 * cavg + 2e-6, (theta, avg, cavg)
     assert mx <= 1.5 * cmx + 1e-5, (theta, mx, cmx)
+
+
+def test_reference_opening_rule_flag(nb, oracle):
+    """NB_FLAG_BH_REFERENCE_OPENING adds the reference's rule (of every opened
+    node, the child toward the body is opened too): more interactions than the
+    default opening test and no less accurate than the CPU tree, which follows
+    the same rule; the default stays within twice the CPU tree's mean error."""
+    state = nb.plummer(16384, seed=2)
+    x, y, z, m = state[0], state[1], state[2], state[6]
+    ref = oracle.forces_naive(x, y, z, m, 1.0, 1e-3)
+    cavg, _ = _errors(oracle.forces_bh_opt(x, y, z, m, 1.0, 1e-3, 0.5, 8), ref)
+    out = {}
+    for name, flags in (("reference", nb.BH_REFERENCE_OPENING), ("plain", 0)):
+        cfg = nb.Config(method=nb.BARNES_HUT, G=1.0, softening=1e-3, theta=0.5,
+                        leaf_capacity=8, flags=flags)
+        with nb.Sim(cfg, capacity=len(x)) as s:
+            s.load(*state)
+            s.compute_forces()
+            info = s.bh_info()
+            out[name] = (_errors(s.accelerations(), ref)[0],
+                         info["interactions_m2p"] + info["interactions_p2p"])
+    assert out["plain"][1] < out["reference"][1]
+    assert out["reference"][0] <= cavg + 2e-6, (out, cavg)
+    assert out["reference"][0] <= out["plain"][0] <= 2.0 * cavg, (out, cavg)
 
 
 def test_theta_zero_is_direct_sum(nb, oracle):
@@ -367,24 +392,30 @@ def test_configuration_size_disk_bulge_2_20(nb, oracle):
     exact fast path and the gallop build hardest.
       - Morton codes, sort order and the whole node table are bit-exact
         against the oracle;
-      - forces of 2048 sampled bodies against the oracle's FP64 direct sum:
-        the mean relative error is no worse than that of the reference's CPU
-        node-pool tree (CPU/src/force_calculator_barnes_hut_optimized.cpp,
-        restated in the oracle) on the same input, and the 99th percentile is
-        within 1.5x of the CPU tree's."""
+      - forces of 2048 sampled bodies against the oracle's FP64 direct sum,
+        beside the reference's CPU node-pool tree
+        (CPU/src/force_calculator_barnes_hut_optimized.cpp, restated in the
+        oracle) on the same input: with the reference's opening rule
+        (NB_FLAG_BH_REFERENCE_OPENING) the mean relative error is no worse
+        than the CPU tree's and the 99th percentile within 1.5x of it; with
+        the default opening test alone (fewer interactions) the mean is within
+        1.5x of the CPU tree's."""
     n, leaf, theta, eps = 1 << 20, 8, 0.5, 1e-3
     state = nb.disk_bulge(n, seed=0)
     x, y, z, m = state[0], state[1], state[2], state[6]
     sc, order, t, root, levels = oracle_tree(oracle, x, y, z, leaf)
-    with bh_sim(nb, state, eps=eps, theta=theta, leaf=leaf) as s:
-        info = s.bh_build()
-        codes, gorder = s.bh_order()
-        assert info["root"] == list(root)
-        assert np.array_equal(codes, sc)
-        assert np.array_equal(gorder, order)
-        nodes = s.bh_nodes(info["num_nodes"])
-        s.compute_forces()
-        a = s.accelerations()
+    acc = {}
+    for name, flags in (("default", 0), ("reference", nb.BH_REFERENCE_OPENING)):
+        with bh_sim(nb, state, eps=eps, theta=theta, leaf=leaf, flags=flags) as s:
+            if name == "default":
+                info = s.bh_build()
+                codes, gorder = s.bh_order()
+                assert info["root"] == list(root)
+                assert np.array_equal(codes, sc)
+                assert np.array_equal(gorder, order)
+                nodes = s.bh_nodes(info["num_nodes"])
+            s.compute_forces()
+            acc[name] = s.accelerations()
     assert info["num_nodes"] == len(t["depth"])
     got = np.lexsort((nodes["is_leaf"], nodes["count"], nodes["first"], nodes["prefix"],
                       nodes["depth"]))
@@ -400,12 +431,14 @@ def test_configuration_size_disk_bulge_2_20(nb, oracle):
     ref = oracle.forces_naive_rows(x[perm], y[perm], z[perm], m[perm], 1.0, eps, 0, len(rows))
     cpu = oracle.forces_bh_opt(x, y, z, m, 1.0, eps, theta, leaf)
 
-    def rel(acc):
-        d = np.sqrt(sum((u[rows] - v) ** 2 for u, v in zip(acc, ref)))
+    def rel(a):
+        d = np.sqrt(sum((u[rows] - v) ** 2 for u, v in zip(a, ref)))
         return d / np.sqrt(sum(v * v for v in ref))
 
-    g, c = rel(a), rel(cpu)
-    print(f"GPU mean {g.mean():.4g} p99 {np.quantile(g, 0.99):.4g} max {g.max():.4g}; "
-          f"CPU tree mean {c.mean():.4g} p99 {np.quantile(c, 0.99):.4g} max {c.max():.4g}")
+    c, g, d = rel(cpu), rel(acc["reference"]), rel(acc["default"])
+    print(f"CPU tree mean {c.mean():.4g} p99 {np.quantile(c, 0.99):.4g}; GPU reference rule "
+          f"mean {g.mean():.4g} p99 {np.quantile(g, 0.99):.4g}; GPU default mean "
+          f"{d.mean():.4g} p99 {np.quantile(d, 0.99):.4g}")
     assert g.mean() <= c.mean() + 2e-6
     assert np.quantile(g, 0.99) <= 1.5 * np.quantile(c, 0.99)
+    assert d.mean() <= 1.5 * c.mean()
