@@ -66,7 +66,7 @@ __host__ __device__ __forceinline__ D4 d4_add(const D4 &a, const D4 &b)
 }
 
 struct BHRoot {
-    double cx, cy, cz, size;        // root cube
+    double cx, cy, cz, size;        // root cube (bh_*_order hand out &cx: centre, then side)
     double off[kMaxLevels];         // child-centre offset below depth l: size * 2^-(l+2)
     float size2[kMaxLevels + 1];    // squared side of a depth-d cell (opening test)
     int levels;                     // depths the root may split into (<= 21)

@@ -50,6 +50,7 @@
 #include "nb_pair.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -123,9 +124,25 @@ struct WarpGeom {
     float thr2, thr2v, thr2x;
 };
 
+// The global cap of the left-out radius, squared: kExactSpacing times the
+// mean body spacing of the root cube, (side^3 / n)^(1/3).  A warp of sparse
+// bodies spread over a large box would otherwise get a radius that takes in
+// whole dense regions, whose terms are a tiny part of its bodies' sums.
+// per_n = kExactSpacing2 n^(-2/3), computed on the host.
+__device__ __forceinline__ float exact_cap2(const double *__restrict__ root, float per_n)
+{
+    const float side = __double2float_rn(root[3]);
+    return __fmul_rn(__fmul_rn(side, side), per_n);
+}
+
+float exact_cap_per_n(int n)
+{
+    return (float)((double)kExactSpacing2 / std::cbrt((double)n * (double)n));
+}
+
 template <int IPT>
 __device__ __forceinline__ WarpGeom warp_geometry(const float4 *__restrict__ box, int tile0,
-                                                  int nchunks, float far2)
+                                                  int nchunks, float far2, float cap2)
 {
     WarpGeom g;
 #pragma unroll
@@ -154,15 +171,14 @@ __device__ __forceinline__ WarpGeom warp_geometry(const float4 *__restrict__ box
     g.thr2v = __fmul_rn(kVeryFar2, diam2);  // very far: Newton step not needed
     // Pairs closer than R leave the FP32 sum and are evaluated in double-single
     // by exact_pairs_kernel (only chunks nearer than R can hold one):
-    // R = min(kExact D, kExactSpacing s), s the mean body spacing of the warp's
-    // box, (V / 64)^(1/3) with every side padded by D / 16 so that a flat box
-    // keeps its in-plane spacing.  The spacing cap keeps sparse warps with
-    // large boxes from sending many pairs.
+    // R = min(kExact D, kExactSpacing s, the global cap), s the mean body
+    // spacing of the warp's box, (V / 64)^(1/3) with every side padded by D / 16
+    // so that a flat box keeps its in-plane spacing.
     const float pad = __fmul_rn(0.0625f, sqrtf(diam2));
     const float vol = __fmul_rn(__fmul_rn(__fadd_rn(side[0], pad), __fadd_rn(side[1], pad)),
                                 __fadd_rn(side[2], pad));
     const float s2 = exp2f(__fmul_rn(0.6666667f, log2f(__fmul_rn(vol, 1.0f / (32.0f * IPT)))));
-    g.thr2x = fminf(__fmul_rn(kExact2, diam2), __fmul_rn(kExactSpacing2, s2));
+    g.thr2x = fminf(fminf(__fmul_rn(kExact2, diam2), __fmul_rn(kExactSpacing2, s2)), cap2);
     return g;
 }
 
@@ -185,7 +201,7 @@ __global__ void __launch_bounds__(WARPS * 32)
 direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                      const float4 *__restrict__ box, int n, int nchunks, float eps2,
                      int seg_chunks, float *__restrict__ psum, float *__restrict__ pcomp,
-                     float far2)
+                     float far2, const double *__restrict__ root, float cap_per_n)
 {
     __shared__ PairTile stage[WARPS];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -193,7 +209,7 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
     if (tile0 >= nchunks) return;
     PairTile &sg = stage[w];
 
-    const WarpGeom gm = warp_geometry<IPT>(box, tile0, nchunks, far2);
+    const WarpGeom gm = warp_geometry<IPT>(box, tile0, nchunks, far2, exact_cap2(root, cap_per_n));
     const float cx = gm.c[0], cy = gm.c[1], cz = gm.c[2];
     const float thr2 = gm.thr2, thr2v = gm.thr2v, thr2x = gm.thr2x;
     const float thrx = __fadd_rn(thr2x, eps2);
@@ -350,7 +366,8 @@ template <int IPT>
 __global__ void __launch_bounds__(kExactWarps * 32)
 exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                    const float4 *__restrict__ box, int n, int nchunks, float eps2, float far2,
-                   double eps2d, double *__restrict__ ex)
+                   double eps2d, const double *__restrict__ root, float cap_per_n,
+                   double *__restrict__ ex)
 {
     __shared__ PairTile stage[kExactWarps];
     __shared__ float ibody[IPT * 32][6];                      // (S, E) of x, y, z
@@ -362,7 +379,7 @@ exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
     const int tile0 = wg * IPT;
     if (tile0 >= nchunks) return;  // the whole CTA
     PairTile &sg = stage[w];
-    const WarpGeom gm = warp_geometry<IPT>(box, tile0, nchunks, far2);
+    const WarpGeom gm = warp_geometry<IPT>(box, tile0, nchunks, far2, exact_cap2(root, cap_per_n));
     const float thrx = __fadd_rn(gm.thr2x, eps2);
     const float2 e2 = dup2(eps2);
     const DS e2ds{__double2float_rn(eps2d),
@@ -650,34 +667,41 @@ int sorted_slots_for(int warps, int ipt)
 template <int W, int I>
 void launch_sorted_shape(dim3 grid, cudaStream_t st, const float4 *hi, const float4 *lo,
                          const float4 *box, int n, double eps2, int seg_chunks, float *psum,
-                         float *pcomp)
+                         float *pcomp, const double *root)
 {
     const int nchunks = (n + kChunk - 1) / kChunk;
     if (eps2 > 0.0)
         direct_sorted_kernel<W, I, false><<<grid, W * 32, 0, st>>>(
-            hi, lo, box, n, nchunks, (float)eps2, seg_chunks, psum, pcomp, kFarFactor2);
+            hi, lo, box, n, nchunks, (float)eps2, seg_chunks, psum, pcomp, kFarFactor2, root,
+            exact_cap_per_n(n));
     else
         direct_sorted_kernel<W, I, true><<<grid, W * 32, 0, st>>>(
-            hi, lo, box, n, nchunks, 0.0f, seg_chunks, psum, pcomp, kFarFactor2);
+            hi, lo, box, n, nchunks, 0.0f, seg_chunks, psum, pcomp, kFarFactor2, root,
+            exact_cap_per_n(n));
 }
 
 // DirectPlan fields here: block = threads per CTA (32 * warps), ipt = chunks
 // per warp, seg_tiles = j-chunks per segment.
 bool launch_sorted(const DirectPlan &p, cudaStream_t st, const float4 *hi, const float4 *lo,
-                   const float4 *box, int n, double eps2, float *psum, float *pcomp)
+                   const float4 *box, int n, double eps2, float *psum, float *pcomp,
+                   const double *root)
 {
     const int warps = p.block / 32;
     const int nchunks = (n + kChunk - 1) / kChunk;
     const int per_cta = warps * p.ipt;
     const dim3 grid((nchunks + per_cta - 1) / per_cta, p.segments);
     if (warps == 4 && p.ipt == 2)
-        launch_sorted_shape<4, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
+        launch_sorted_shape<4, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp,
+                                  root);
     else if (warps == 8 && p.ipt == 2)
-        launch_sorted_shape<8, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
+        launch_sorted_shape<8, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp,
+                                  root);
     else if (warps == 2 && p.ipt == 2)
-        launch_sorted_shape<2, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
+        launch_sorted_shape<2, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp,
+                                  root);
     else if (warps == 1 && p.ipt == 2)
-        launch_sorted_shape<1, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp);
+        launch_sorted_shape<1, 2>(grid, st, hi, lo, box, n, eps2, p.seg_tiles, psum, pcomp,
+                                  root);
     else
         return false;
     return true;
@@ -743,7 +767,7 @@ static nb_status run_sorted(const DirectPlan &p, const float4 *hi, const float4 
     NB_TRY(b.partials.reserve(sizeof(float) * 6 * (size_t)n * p.segments));
     float *psum = b.partials.as<float>();
     float *pcomp = psum + 3 * (size_t)n * p.segments;
-    if (!launch_sorted(p, st, hi, lo, b.boxes.as<float4>(), n, eps2, psum, pcomp))
+    if (!launch_sorted(p, st, hi, lo, b.boxes.as<float4>(), n, eps2, psum, pcomp, b.centre))
         return fail(NB_ERR_UNSUPPORTED, "direct_mixed_sorted: unsupported tile shape");
     NB_LAUNCH_CHECK();
     *psum_out = psum;
@@ -770,7 +794,7 @@ static nb_status launch_exact_pairs(const float4 *hi, const float4 *lo, int n, d
     const int nchunks = (n + kChunk - 1) / kChunk;
     exact_pairs_kernel<kIpt><<<sorted_warps(n), kExactWarps * 32, 0, b.side>>>(
         hi, lo, b.boxes.as<float4>(), n, nchunks, eps2 > 0.0 ? (float)eps2 : 0.0f, kFarFactor2,
-        eps2 > 0.0 ? eps2 : 0.0, b.exact.as<double>());
+        eps2 > 0.0 ? eps2 : 0.0, b.centre, exact_cap_per_n(n), b.exact.as<double>());
     NB_LAUNCH_CHECK();
     NB_CUDA_TRY(cudaEventRecord(b.join, b.side));
     return NB_OK;

@@ -272,7 +272,8 @@ void bh_mark_count_stale(BHTree *t);
 nb_status bh_info(BHTree *t, cudaStream_t st, nb_bh_info *info);
 // Morton order of the bodies by the top 3*levels code bits: *order maps a
 // sorted index to the original one; *root_centre points at the device copy of
-// the root cube centre (3 doubles).  Both stay valid until the next call on t.
+// the root cube centre (3 doubles), followed by the cube's side (a 4th
+// double).  Both stay valid until the next call on t.
 nb_status bh_morton_order(BHTree *t, const double *x, const double *y, const double *z, int n,
                           int levels, cudaStream_t st, const uint32_t **order,
                           const double **root_centre);
