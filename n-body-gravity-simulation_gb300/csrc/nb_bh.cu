@@ -1102,6 +1102,251 @@ walk2_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
     }
 }
 
+// ------------------------------------------------------------ child groups
+// The group walk reads the children of a node together: gnodes holds, for
+// every internal node, its children's records contiguously and in Morton order
+// (a group), and group 0 is the root alone.  count_kids_kernel counts each
+// node's children and claims a place for its group from a counter (every node
+// but the root is the child of exactly one node, so there are as many records
+// as nodes; where a group lands changes no result, since the walk's arithmetic
+// follows the groups' contents), and group_kernel writes each record with its
+// children count, its parent centre and, for the quadrupole walk, its
+// quadrupole beside it.  Both run over the node count read on the device.
+struct alignas(32) BHGNode {
+    float4 com_mass;  // as BHNode
+    float size2;
+    int first, count;
+    int kids;         // the record of the node's first child (-1: a leaf)
+};
+static_assert(sizeof(BHGNode) == 32, "group record layout");
+
+__global__ void __launch_bounds__(256)
+count_kids_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
+                  int *__restrict__ nkids, int *__restrict__ base, int *__restrict__ next)
+{
+    const int num = *total;
+    for (int k = blockIdx.x * 256 + threadIdx.x; k < num; k += gridDim.x * 256) {
+        const int skip = nodes[k].skip;  // the children: k + 1, then skip pointers up to it
+        int c = 0;
+        for (int ch = k + 1; ch < skip && c < 8; ch = nodes[ch].skip) ++c;
+        nkids[k] = c;
+        if (c > 0) base[k] = atomicAdd(next, c);
+    }
+}
+
+__global__ void __launch_bounds__(256)
+group_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
+             const int *__restrict__ nkids, const int *__restrict__ base,
+             const float4 *__restrict__ pcen, const float4 *__restrict__ quad,
+             BHGNode *__restrict__ gnodes, unsigned char *__restrict__ gnk,
+             float4 *__restrict__ gpcen, float4 *__restrict__ gquad)
+{
+    const int num = *total;
+    // record pos := node x
+    auto put = [&](int pos, int x) {
+        if (!NB_IN_RANGE(pos, num) || !NB_IN_RANGE(x, num)) return;
+        const BHNode nd = nodes[x];
+        const int nk = nkids[x];
+        BHGNode g;
+        g.com_mass = nd.com_mass;
+        g.size2 = nd.size2;
+        g.first = nd.first;
+        g.count = nd.count;
+        g.kids = nk > 0 ? 1 + base[x] : -1;
+        gnodes[pos] = g;
+        gnk[pos] = (unsigned char)nk;
+        gpcen[pos] = pcen[x];
+        if (quad) {
+            gquad[2 * pos] = quad[2 * x];
+            gquad[2 * pos + 1] = quad[2 * x + 1];
+        }
+    };
+    for (int k = blockIdx.x * 256 + threadIdx.x; k < num; k += gridDim.x * 256) {
+        if (k == 0) put(0, 0);
+        const int nk = nkids[k];
+        int ch = k + 1;
+        for (int r = 0; r < nk; ++r) {
+            put(1 + base[k] + r, ch);
+            ch = nodes[ch].skip;
+        }
+    }
+}
+
+// A depth-first walk over groups keeps, per level of its current path, at most
+// 7 groups of unvisited siblings, plus the at most 8 groups the last group
+// pushed; groups lie at levels 0 .. kMaxLevels.
+constexpr int kGroupBlock = 32;  // threads of a group-walk CTA
+constexpr int kWalkWarps = kGroupBlock / 32;
+constexpr int kGroupStack = 8 * (kMaxLevels + 1);
+
+// The walk of walk2_kernel (64 NP bodies per warp, 2 NP per lane as packed
+// pairs; the same opening rule, decided for the whole warp) over child groups:
+// one round trip to memory brings a group's records into the warp's shared
+// memory, and the warp then tests the children one after the other, adding
+// the monopoles of the children no body opens, summing opened leaves' bodies,
+// and pushing the groups of opened internal children onto its stack.  The
+// interactions are those of walk2_kernel; only their order differs.
+template <bool ZERO_SOFT, bool QUAD, int NP, bool DIR>
+__global__ void __launch_bounds__(kGroupBlock)
+group_walk_kernel(const BHGNode *__restrict__ gnodes, const unsigned char *__restrict__ gnk,
+                  const int *__restrict__ total, const float4 *__restrict__ body,
+                  const uint32_t *__restrict__ order, int n, float theta2, float eps2, double G,
+                  double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
+                  BHStats *__restrict__ stats, const float4 *__restrict__ gquad,
+                  const float4 *__restrict__ gpcen)
+{
+    __shared__ BHGNode s_rec[kWalkWarps][8];
+    __shared__ float4 s_quad[kWalkWarps][QUAD ? 16 : 1];
+    __shared__ float4 s_pc[kWalkWarps][DIR ? 8 : 1];
+    __shared__ int2 s_stack[kWalkWarps][kGroupStack];
+    constexpr int kPer = 64 * NP;  // bodies per warp
+    const int num_nodes = *total;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int w0 = ((blockIdx.x * kGroupBlock + threadIdx.x) >> 5) * kPer;
+    if (w0 >= n) return;  // whole warp past the end
+    const int wend = min(n, w0 + kPer);  // the warp's bodies: [w0, wend)
+    int ia[NP], ib[NP];
+    bool va[NP], vb[NP];
+    float2 npx[NP], npy[NP], npz[NP], fx[NP], fy[NP], fz[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        ia[k] = w0 + 64 * k + lane;
+        ib[k] = ia[k] + 32;
+        va[k] = ia[k] < n;
+        vb[k] = ib[k] < n;
+        // a slot past n walks with body w0: its tests repeat that body's
+        const float4 pa = body[va[k] ? ia[k] : w0], pb = body[vb[k] ? ib[k] : w0];
+        npx[k] = make_float2(-pa.x, -pb.x);
+        npy[k] = make_float2(-pa.y, -pb.y);
+        npz[k] = make_float2(-pa.z, -pb.z);
+        fx[k] = fy[k] = fz[k] = dup2(0.f);
+    }
+    const float2 e2 = dup2(eps2), t2 = dup2(theta2);
+    unsigned m2p = 0, p2p = 0;
+    int sp = 1;
+    if (lane == 0) s_stack[w][0] = make_int2(0, 1);
+    while (sp > 0) {
+        __syncwarp();
+        const int2 g = s_stack[w][--sp];
+        if (!NB_IN_RANGE(g.x + g.y - 1, num_nodes)) break;
+        int mynk = 0;
+        if (lane < g.y) {
+            s_rec[w][lane] = gnodes[g.x + lane];
+            mynk = gnk[g.x + lane];
+            if (DIR) s_pc[w][lane] = gpcen[g.x + lane];
+        }
+        if (QUAD && lane < 2 * g.y) s_quad[w][lane] = gquad[2 * g.x + lane];
+        __syncwarp();
+        for (int c = 0; c < g.y; ++c) {
+            const BHGNode nd = s_rec[w][c];
+            const float4 pc = DIR ? s_pc[w][c] : make_float4(0.f, 0.f, 0.f, 0.f);
+            float2 dx[NP], dy[NP], dz[NP], d2[NP];
+            // a node that holds one of the warp's bodies is opened (each body's
+            // own cell); the others by the opening test of any body
+            bool open = nd.first < wend && nd.first + nd.count > w0;
+#pragma unroll
+            for (int k = 0; k < NP; ++k) {
+                dx[k] = add2(dup2(nd.com_mass.x), npx[k]);
+                dy[k] = add2(dup2(nd.com_mass.y), npy[k]);
+                dz[k] = add2(dup2(nd.com_mass.z), npz[k]);
+                d2[k] = fma2(dz[k], dz[k], fma2(dy[k], dy[k], mul2(dx[k], dx[k])));
+                const float2 td2 = mul2(t2, d2[k]);
+                open = open | (nd.size2 >= td2.x) | (nd.size2 >= td2.y);
+                if (DIR)
+                    open = open | toward_body(pc, -npx[k].x, -npy[k].x, -npz[k].x) |
+                           toward_body(pc, -npx[k].y, -npy[k].y, -npz[k].y);
+            }
+            if (__any_sync(0xffffffffu, open)) {
+                if (nd.kids >= 0) {  // internal: its children's group, later
+                    const int nk = __shfl_sync(0xffffffffu, mynk, c);
+                    if (NB_IN_RANGE(sp, kGroupStack) && sp < kGroupStack) {
+                        if (lane == 0) s_stack[w][sp] = make_int2(nd.kids, nk);
+                        ++sp;
+                    }
+                    continue;
+                }
+                const int e = NB_IN_RANGE(nd.first, n) && NB_IN_RANGE(nd.first + nd.count - 1, n)
+                                  ? nd.first + nd.count
+                                  : nd.first;
+#pragma unroll 2
+                for (int b = nd.first; b < e; ++b) {
+                    const float4 q = body[b];
+#pragma unroll
+                    for (int k = 0; k < NP; ++k) {
+                        const float2 rx = add2(dup2(q.x), npx[k]);
+                        const float2 ry = add2(dup2(q.y), npy[k]);
+                        const float2 rz = add2(dup2(q.z), npz[k]);
+                        const float2 r2 = fma2(rz, rz, fma2(ry, ry, fma2(rx, rx, e2)));
+                        float2 inv = make_float2(rsqrt_mufu(r2.x), rsqrt_mufu(r2.y));
+                        if (ZERO_SOFT) {
+                            inv.x = r2.x > 0.f ? inv.x : 0.f;
+                            inv.y = r2.y > 0.f ? inv.y : 0.f;
+                        }
+                        const float2 s = mul2(mul2(dup2(q.w), inv), mul2(inv, inv));
+                        fx[k] = fma2(rx, s, fx[k]);
+                        fy[k] = fma2(ry, s, fy[k]);
+                        fz[k] = fma2(rz, s, fz[k]);
+                    }
+                }
+                p2p += nd.count;
+            } else {
+                float4 q0, q1;
+                if (QUAD) {
+                    q0 = s_quad[w][2 * c];
+                    q1 = s_quad[w][2 * c + 1];
+                }
+#pragma unroll
+                for (int k = 0; k < NP; ++k) {
+                    const float2 r2 = add2(d2[k], e2);
+                    const float2 inv = make_float2(rsqrt_mufu(r2.x), rsqrt_mufu(r2.y));
+                    const float2 inv2 = mul2(inv, inv);
+                    const float2 s = mul2(mul2(dup2(nd.com_mass.w), inv), inv2);
+                    fx[k] = fma2(dx[k], s, fx[k]);
+                    fy[k] = fma2(dy[k], s, fy[k]);
+                    fz[k] = fma2(dz[k], s, fz[k]);
+                    if (QUAD) {
+                        const float2 qx = fma2(dup2(q0.x), dx[k],
+                                               fma2(dup2(q0.w), dy[k], mul2(dup2(q1.x), dz[k])));
+                        const float2 qy = fma2(dup2(q0.w), dx[k],
+                                               fma2(dup2(q0.y), dy[k], mul2(dup2(q1.y), dz[k])));
+                        const float2 qz = fma2(dup2(q1.x), dx[k],
+                                               fma2(dup2(q1.y), dy[k], mul2(dup2(q0.z), dz[k])));
+                        const float2 rqr = fma2(dx[k], qx, fma2(dy[k], qy, mul2(dz[k], qz)));
+                        const float2 inv5 = mul2(mul2(inv, inv2), inv2);
+                        const float2 f = mul2(mul2(dup2(2.5f), rqr), inv2);
+                        fx[k] = fma2(inv5, fma2(f, dx[k], make_float2(-qx.x, -qx.y)), fx[k]);
+                        fy[k] = fma2(inv5, fma2(f, dy[k], make_float2(-qy.x, -qy.y)), fy[k]);
+                        fz[k] = fma2(inv5, fma2(f, dz[k], make_float2(-qz.x, -qz.y)), fz[k]);
+                    }
+                }
+                ++m2p;
+            }
+        }
+    }
+    unsigned nv = 0;
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        if (va[k]) {
+            const uint32_t o = order[ia[k]];
+            ax[o] = G * (double)fx[k].x;
+            ay[o] = G * (double)fy[k].x;
+            az[o] = G * (double)fz[k].x;
+        }
+        if (vb[k]) {
+            const uint32_t o = order[ib[k]];
+            ax[o] = G * (double)fx[k].y;
+            ay[o] = G * (double)fy[k].y;
+            az[o] = G * (double)fz[k].y;
+        }
+        nv += __popc(__ballot_sync(0xffffffffu, va[k])) + __popc(__ballot_sync(0xffffffffu, vb[k]));
+    }
+    if (lane == 0) {
+        atomicAdd(&stats->m2p, (unsigned long long)m2p * nv);
+        atomicAdd(&stats->p2p, (unsigned long long)p2p * nv);
+        atomicAdd(&stats->total, (unsigned long long)(m2p + p2p) * nv);
+    }
+}
+
 int div_up(long a, long b) { return (int)((a + b - 1) / b); }
 
 template <class T>
@@ -1129,7 +1374,7 @@ struct BHTree {
     cudaEvent_t total_ready = nullptr;
     DevBuf part, root, keys0, keys1, vals0, vals1, hist, body, moments, prefix, chain_len,
         chain_depth, offsets, scan_tmp, nodes, node_depth, boxes, stats, moments2a, moments2b,
-        prefix2a, prefix2b, quad, pcen;
+        prefix2a, prefix2b, quad, pcen, nkids, kbase, gnodes, gnk, gpcen, gquad;
     bool with_quad = false;     // the nodes carry quadrupoles (quad, 2 float4 per node)
     bool ref_open = false;      // the reference's opening rule (the child toward the body too)
     const uint64_t *sorted_codes = nullptr;
@@ -1157,7 +1402,8 @@ void bh_destroy(BHTree *t)
                       &t->hist, &t->body, &t->moments, &t->prefix, &t->chain_len,
                       &t->chain_depth, &t->offsets, &t->scan_tmp, &t->nodes, &t->node_depth,
                       &t->boxes, &t->stats, &t->moments2a, &t->moments2b, &t->prefix2a,
-                      &t->prefix2b, &t->quad, &t->pcen};
+                      &t->prefix2b, &t->quad, &t->pcen, &t->nkids, &t->kbase, &t->gnodes,
+                      &t->gnk, &t->gpcen, &t->gquad};
     for (DevBuf *b : bufs) b->release();
     if (t->h_total) cudaFreeHost(t->h_total);
     if (t->total_ready) cudaEventDestroy(t->total_ready);
@@ -1319,13 +1565,33 @@ int walk_pairs()
     return np;
 }
 
+// The walk over child groups (default) or the stackless preorder walk
+// (NB_BH_WALK=preorder, read at every walk; both find the same interactions).
+bool group_walk()
+{
+    const char *e = std::getenv("NB_BH_WALK");
+    return !(e && std::strcmp(e, "preorder") == 0);
+}
+
 template <bool ZS, bool Q, bool D>
 void walk_launch(BHTree *t, int n, float theta2, float eps2, double G, double *ax, double *ay,
                  double *az, cudaStream_t st)
 {
     const int np = walk_pairs();
     const float4 *pc = t->pcen.as<float4>();
-    if (np == 2)
+    if (group_walk() && np >= 1) {
+        const BHGNode *gn = t->gnodes.as<BHGNode>();
+        const unsigned char *gk = t->gnk.as<unsigned char>();
+        const float4 *gq = t->gquad.as<float4>(), *gp = t->gpcen.as<float4>();
+        if (np == 2)
+            group_walk_kernel<ZS, Q, 2, D><<<div_up(n, 4 * kGroupBlock), kGroupBlock, 0, st>>>(
+                gn, gk, d_total(t), t->body.as<float4>(), t->order, n, theta2, eps2, G, ax, ay,
+                az, t->stats.as<BHStats>(), gq, gp);
+        else
+            group_walk_kernel<ZS, Q, 1, D><<<div_up(n, 2 * kGroupBlock), kGroupBlock, 0, st>>>(
+                gn, gk, d_total(t), t->body.as<float4>(), t->order, n, theta2, eps2, G, ax, ay,
+                az, t->stats.as<BHStats>(), gq, gp);
+    } else if (np == 2)
         walk2_kernel<ZS, Q, 2, D><<<div_up(n, 4 * kWalkBlock), kWalkBlock, 0, st>>>(
             t->nodes.as<BHNode>(), d_total(t), t->body.as<float4>(), t->order, n, theta2,
             eps2, G, ax, ay, az, t->stats.as<BHStats>(), t->quad.as<float4>(), pc);
@@ -1389,6 +1655,35 @@ static nb_status compute_quads(BHTree *t, const double *x, const double *y, cons
     return NB_OK;
 }
 
+// The child-group records of the current tree (after its monopoles, sides
+// and quadrupoles); recount: a new topology (children counts and group
+// places), else only the records are rewritten.
+static nb_status group_nodes(BHTree *t, cudaStream_t st, bool recount)
+{
+    const int slots = launch_nodes(t);
+    const int grid = std::max(1, std::min(div_up(slots, 256), 8 * device_props().num_sms));
+    if (recount) {
+        NB_TRY(t->nkids.reserve(sizeof(int) * (size_t)slots));
+        NB_TRY(t->kbase.reserve(sizeof(int) * ((size_t)slots + 1)));
+        int *next = t->kbase.as<int>() + slots;  // the group counter (group 0: the root)
+        NB_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(int), st));
+        count_kids_kernel<<<grid, 256, 0, st>>>(t->nodes.as<BHNode>(), d_total(t),
+                                                t->nkids.as<int>(), t->kbase.as<int>(), next);
+        NB_LAUNCH_CHECK();
+    }
+    NB_TRY(t->gnodes.reserve(sizeof(BHGNode) * (size_t)slots));
+    NB_TRY(t->gnk.reserve((size_t)slots));
+    NB_TRY(t->gpcen.reserve(sizeof(float4) * (size_t)slots));
+    if (t->with_quad) NB_TRY(t->gquad.reserve(sizeof(float4) * 2 * (size_t)slots));
+    group_kernel<<<grid, 256, 0, st>>>(
+        t->nodes.as<BHNode>(), d_total(t), t->nkids.as<int>(), t->kbase.as<int>(),
+        t->pcen.as<float4>(), t->with_quad ? t->quad.as<float4>() : nullptr,
+        t->gnodes.as<BHGNode>(), t->gnk.as<unsigned char>(), t->gpcen.as<float4>(),
+        t->with_quad ? t->gquad.as<float4>() : nullptr);
+    NB_LAUNCH_CHECK();
+    return NB_OK;
+}
+
 // Monopoles and cell sides of the kept topology for the current positions.
 static nb_status refit(BHTree *t, const double *x, const double *y, const double *z,
                        const double *m, int n, cudaStream_t st)
@@ -1430,6 +1725,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     if (ax && reuse > 1 && t->tree_valid && t->n == n && t->evals_since_build < reuse) {
         NB_TRY(refit(t, x, y, z, m, n, st));
         if (quad) NB_TRY(compute_quads(t, x, y, z, m, n, st));
+        NB_TRY(group_nodes(t, st, false));
         ++t->evals_since_build;
         return launch_walk(t, n, G, eps2, theta, ax, ay, az, st, timer);
     }
@@ -1494,6 +1790,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
                                                 t->pcen.as<float4>(), stats, t->node_cap);
     NB_LAUNCH_CHECK();
     if (quad) NB_TRY(compute_quads(t, x, y, z, m, n, st));
+    NB_TRY(group_nodes(t, st, true));
     t->tree_valid = true;
     t->evals_since_build = 0;
     if (!ax) return NB_OK;
