@@ -457,8 +457,12 @@ template <> struct Add<D4> {
     __device__ static D4 op(const D4 &a, const D4 &b) { return d4_add(a, b); }
 };
 
-constexpr int kScanItems = 4;
-constexpr int kScanTile = 256 * kScanItems;
+// Elements per thread of the scans: more for the FP64 moments, whose warp
+// and block steps run on GB300's narrow FP64 pipe, so fewer of them per
+// element pays.
+template <class T> struct ScanItems { static constexpr int n = 4; };
+template <> struct ScanItems<D4> { static constexpr int n = 8; };
+template <class T> __host__ __device__ constexpr int scan_tile() { return 256 * ScanItems<T>::n; }
 
 __device__ __forceinline__ int shfl_up(int v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
 __device__ __forceinline__ D4 shfl_up(const D4 &v, int d)
@@ -506,18 +510,19 @@ __device__ __forceinline__ T block_exclusive(T s, T *warp_sums, T *total)
     return Add<T>::op(warp_sums[warp], excl);
 }
 
-// sums[b] = the sum of tile b (kScanTile elements): a tree in shared memory,
+// sums[b] = the sum of tile b (scan_tile<T>() elements): a tree in shared memory,
 // whose idle warps skip their steps (fewer FP64 adds than a shuffle
 // reduction, in which every lane adds at every step).
 template <class T>
 __global__ void __launch_bounds__(256)
 scan_reduce_kernel(const T *__restrict__ in, int n, T *__restrict__ sums)
 {
+    constexpr int kItems = ScanItems<T>::n;
     __shared__ T sh[256];
-    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    const int base = blockIdx.x * scan_tile<T>() + threadIdx.x * kItems;
     T s = Add<T>::zero();
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k)
+    for (int k = 0; k < kItems; ++k)
         if (base + k < n) s = Add<T>::op(s, in[base + k]);
     sh[threadIdx.x] = s;
     __syncthreads();
@@ -553,21 +558,22 @@ __global__ void __launch_bounds__(256)
 scan_apply_kernel(const T *__restrict__ in, int n, const T *__restrict__ block_off,
                   T *__restrict__ out)
 {
+    constexpr int kItems = ScanItems<T>::n;
     __shared__ T warp_sums[9];
-    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
-    T v[kScanItems];
+    const int base = blockIdx.x * scan_tile<T>() + threadIdx.x * kItems;
     T s = Add<T>::zero();
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        v[k] = base + k < n ? in[base + k] : Add<T>::zero();
-        s = Add<T>::op(s, v[k]);
-    }
+    for (int k = 0; k < kItems; ++k)
+        if (base + k < n) s = Add<T>::op(s, in[base + k]);
     T total;
     T run = Add<T>::op(block_off[blockIdx.x], block_exclusive<T, 8>(s, warp_sums, &total));
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        if (base + k < n) out[base + k] = run;
-        run = Add<T>::op(run, v[k]);
+    for (int k = 0; k < kItems; ++k) {  // the thread's elements again (L1)
+        if (base + k < n) {
+            const T v = in[base + k];
+            out[base + k] = run;
+            run = Add<T>::op(run, v);
+        }
         if (base + k == n - 1) out[n] = run;
     }
 }
@@ -624,10 +630,11 @@ __device__ __forceinline__ int cell_start(const uint64_t *__restrict__ c, int i,
 }
 
 // Depth of the first node starting at body i and the length of its chain
-// (0 when no node starts at i).
+// (0 when no node starts at i); pstart[i]: the first body of that node's
+// parent cell (when i starts a chain below the root).
 __global__ void __launch_bounds__(256)
 chain_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__restrict__ root,
-             int *__restrict__ chain_len, int *__restrict__ chain_depth)
+             int *__restrict__ chain_len, int *__restrict__ chain_depth, int *__restrict__ pstart)
 {
     const int i = blockIdx.x * 256 + threadIdx.x;
     if (i >= n) return;
@@ -642,8 +649,10 @@ chain_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__res
             starts = false;
         } else {
             a = s + 1;
-            const int pc = cell_end(c, n, i, s) - cell_start(c, i, s);
+            const int ps = cell_start(c, i, s);
+            const int pc = cell_end(c, n, i, s) - ps;
             starts = pc > cap;
+            pstart[i] = ps;
         }
     }
     if (starts) {
@@ -707,7 +716,9 @@ node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__rest
             const int *__restrict__ chain_len, const int *__restrict__ chain_depth,
             const int *__restrict__ offsets, const D4 *__restrict__ P,
             BHNode *__restrict__ nodes, unsigned char *__restrict__ node_depth,
-            float4 *__restrict__ pcen, BHStats *__restrict__ stats, int node_cap)
+            const int *__restrict__ pstart, int *__restrict__ parent,
+            unsigned char *__restrict__ octant, unsigned *__restrict__ occ,
+            BHStats *__restrict__ stats, int node_cap)
 {
     const int i = blockIdx.x * 256 + threadIdx.x;
     if (i >= n) return;
@@ -730,12 +741,35 @@ node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__rest
         nd.size2 = root->size2[d];
         nodes[id0 + k] = nd;
         node_depth[id0 + k] = (unsigned char)d;
-        pcen[id0 + k] = parent_centre(c[i], d, root);
+        if (d > 0) {  // the parent: the previous node of the chain, or the one holding it
+            int par = id0 + k - 1;
+            if (k == 0) {
+                const int j = pstart[i];
+                par = offsets[j] + (d - 1 - chain_depth[j]);
+            }
+            const int oct = (int)((c[i] >> (63 - 3 * d)) & 7u);
+            parent[id0 + k] = par;
+            octant[id0 + k] = (unsigned char)oct;
+            if (NB_IN_RANGE(par, node_cap)) atomicOr(&occ[par], 1u << oct);
+        }
         leaves += leaf;
         maxd = max(maxd, d);
     }
     if (leaves) atomicAdd(&stats->leaves, leaves);
     atomicMax(&stats->max_depth, maxd);
+}
+
+// Parent centres and octants of every node (parent_centre), for the walk
+// under the reference's opening rule only: read off the Morton code of the
+// node's first body and its depth.
+__global__ void __launch_bounds__(256)
+pcen_kernel(const uint64_t *__restrict__ c, const BHNode *__restrict__ nodes,
+            const unsigned char *__restrict__ node_depth, const int *__restrict__ total,
+            const BHRoot *__restrict__ root, float4 *__restrict__ pcen)
+{
+    const int num = *total;
+    for (int k = blockIdx.x * 256 + threadIdx.x; k < num; k += gridDim.x * 256)
+        pcen[k] = parent_centre(c[nodes[k].first], node_depth[k], root);
 }
 
 // ------------------------------------------------------------ refit
@@ -1105,8 +1139,9 @@ walk2_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
 // ------------------------------------------------------------ child groups
 // The group walk reads the children of a node together: gnodes holds, for
 // every internal node, its children's records contiguously and in Morton order
-// (a group), and group 0 is the root alone.  count_kids_kernel counts each
-// node's children and claims a place for its group from a counter (every node
+// (a group), and group 0 is the root alone.  node_kernel records every node's
+// parent and octant and sets the octant's bit in the parent's mask;
+// alloc_groups_kernel claims a place for each group from a counter (every node
 // but the root is the child of exactly one node, so there are as many records
 // as nodes; where a group lands changes no result, since the walk's arithmetic
 // follows the groups' contents), and group_kernel writes each record with its
@@ -1120,54 +1155,61 @@ struct alignas(32) BHGNode {
 };
 static_assert(sizeof(BHGNode) == 32, "group record layout");
 
+// A place for the group of every node with children (occ: the mask of its
+// non-empty octants): a block numbers its nodes' groups by a scan and claims
+// their span from the counter with one atomic.
 __global__ void __launch_bounds__(256)
-count_kids_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
-                  int *__restrict__ nkids, int *__restrict__ base, int *__restrict__ next)
+alloc_groups_kernel(const unsigned *__restrict__ occ, const int *__restrict__ total,
+                    int *__restrict__ base, int *__restrict__ next)
 {
+    __shared__ int warp_sums[9];
+    __shared__ int span0;
     const int num = *total;
-    for (int k = blockIdx.x * 256 + threadIdx.x; k < num; k += gridDim.x * 256) {
-        const int skip = nodes[k].skip;  // the children: k + 1, then skip pointers up to it
-        int c = 0;
-        for (int ch = k + 1; ch < skip && c < 8; ch = nodes[ch].skip) ++c;
-        nkids[k] = c;
-        if (c > 0) base[k] = atomicAdd(next, c);
+    for (int k0 = blockIdx.x * 256; k0 < num; k0 += gridDim.x * 256) {
+        const int k = k0 + threadIdx.x;
+        const int nk = k < num ? __popc(occ[k]) : 0;
+        int span;
+        const int off = block_exclusive<int, 8>(nk, warp_sums, &span);
+        if (threadIdx.x == 0) span0 = atomicAdd(next, span);
+        __syncthreads();
+        if (nk > 0) base[k] = span0 + off;
+        __syncthreads();  // span0 and warp_sums are reused by the next round
     }
 }
 
+// Every node's record: the root at 0, a child at its parent's group place
+// plus its rank among the parent's non-empty octants (Morton order).
 __global__ void __launch_bounds__(256)
 group_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
-             const int *__restrict__ nkids, const int *__restrict__ base,
+             const unsigned *__restrict__ occ, const int *__restrict__ base,
+             const int *__restrict__ parent, const unsigned char *__restrict__ octant,
              const float4 *__restrict__ pcen, const float4 *__restrict__ quad,
              BHGNode *__restrict__ gnodes, unsigned char *__restrict__ gnk,
              float4 *__restrict__ gpcen, float4 *__restrict__ gquad)
 {
     const int num = *total;
-    // record pos := node x
-    auto put = [&](int pos, int x) {
-        if (!NB_IN_RANGE(pos, num) || !NB_IN_RANGE(x, num)) return;
-        const BHNode nd = nodes[x];
-        const int nk = nkids[x];
+    for (int k = blockIdx.x * 256 + threadIdx.x; k < num; k += gridDim.x * 256) {
+        int pos = 0;
+        if (k > 0) {
+            const int par = parent[k];
+            if (!NB_IN_RANGE(par, num)) continue;
+            pos = 1 + base[par] + __popc(occ[par] & ((1u << octant[k]) - 1u));
+        }
+        if (!NB_IN_RANGE(pos, num)) continue;
+        const BHNode nd = nodes[k];
+        const unsigned o = occ[k];
         BHGNode g;
         g.com_mass = nd.com_mass;
         g.size2 = nd.size2;
         g.first = nd.first;
         g.count = nd.count;
-        g.kids = nk > 0 ? 1 + base[x] : -1;
+        g.kids = o ? 1 + base[k] : -1;
         gnodes[pos] = g;
-        gnk[pos] = (unsigned char)nk;
-        gpcen[pos] = pcen[x];
+        gnk[pos] = (unsigned char)__popc(o);
+        if (pcen) gpcen[pos] = pcen[k];
         if (quad) {
-            gquad[2 * pos] = quad[2 * x];
-            gquad[2 * pos + 1] = quad[2 * x + 1];
-        }
-    };
-    for (int k = blockIdx.x * 256 + threadIdx.x; k < num; k += gridDim.x * 256) {
-        if (k == 0) put(0, 0);
-        const int nk = nkids[k];
-        int ch = k + 1;
-        for (int r = 0; r < nk; ++r) {
-            put(1 + base[k] + r, ch);
-            ch = nodes[ch].skip;
+            gquad[2 * pos] = quad[2 * k];
+            gquad[2 * pos + 1] = quad[2 * k + 1];
         }
     }
 }
@@ -1352,7 +1394,7 @@ int div_up(long a, long b) { return (int)((a + b - 1) / b); }
 template <class T>
 nb_status scan_exclusive(const T *in, int n, T *out, DevBuf &tmp, cudaStream_t st)
 {
-    const int nb = div_up(n, kScanTile);
+    const int nb = div_up(n, scan_tile<T>());
     NB_TRY(tmp.reserve(sizeof(T) * (size_t)std::max(nb, 1)));
     T *sums = tmp.as<T>();
     scan_reduce_kernel<T><<<nb, 256, 0, st>>>(in, n, sums);
@@ -1374,9 +1416,11 @@ struct BHTree {
     cudaEvent_t total_ready = nullptr;
     DevBuf part, root, keys0, keys1, vals0, vals1, hist, body, moments, prefix, chain_len,
         chain_depth, offsets, scan_tmp, nodes, node_depth, boxes, stats, moments2a, moments2b,
-        prefix2a, prefix2b, quad, pcen, nkids, kbase, gnodes, gnk, gpcen, gquad;
+        prefix2a, prefix2b, quad, pcen, pstart, parent, octant, occ, kbase, gnodes, gnk, gpcen,
+        gquad;
     bool with_quad = false;     // the nodes carry quadrupoles (quad, 2 float4 per node)
     bool ref_open = false;      // the reference's opening rule (the child toward the body too)
+    bool pcen_valid = false;    // pcen holds the parent centres of the current topology
     const uint64_t *sorted_codes = nullptr;
     const uint32_t *order = nullptr;
     bool tree_valid = false;    // nodes/order describe a build of these bodies' count
@@ -1402,7 +1446,8 @@ void bh_destroy(BHTree *t)
                       &t->hist, &t->body, &t->moments, &t->prefix, &t->chain_len,
                       &t->chain_depth, &t->offsets, &t->scan_tmp, &t->nodes, &t->node_depth,
                       &t->boxes, &t->stats, &t->moments2a, &t->moments2b, &t->prefix2a,
-                      &t->prefix2b, &t->quad, &t->pcen, &t->nkids, &t->kbase, &t->gnodes,
+                      &t->prefix2b, &t->quad, &t->pcen, &t->pstart, &t->parent, &t->octant,
+                      &t->occ, &t->kbase, &t->gnodes,
                       &t->gnk, &t->gpcen, &t->gquad};
     for (DevBuf *b : bufs) b->release();
     if (t->h_total) cudaFreeHost(t->h_total);
@@ -1655,6 +1700,21 @@ static nb_status compute_quads(BHTree *t, const double *x, const double *y, cons
     return NB_OK;
 }
 
+// The parent centres the reference's opening rule needs, once per topology.
+static nb_status ensure_pcen(BHTree *t, cudaStream_t st)
+{
+    if (!t->ref_open || t->pcen_valid) return NB_OK;
+    const int slots = launch_nodes(t);
+    NB_TRY(t->pcen.reserve(sizeof(float4) * (size_t)slots));
+    const int grid = std::max(1, std::min(div_up(slots, 256), 8 * device_props().num_sms));
+    pcen_kernel<<<grid, 256, 0, st>>>(t->sorted_codes, t->nodes.as<BHNode>(),
+                                      t->node_depth.as<unsigned char>(), d_total(t),
+                                      t->root.as<BHRoot>(), t->pcen.as<float4>());
+    NB_LAUNCH_CHECK();
+    t->pcen_valid = true;
+    return NB_OK;
+}
+
 // The child-group records of the current tree (after its monopoles, sides
 // and quadrupoles); recount: a new topology (children counts and group
 // places), else only the records are rewritten.
@@ -1663,22 +1723,23 @@ static nb_status group_nodes(BHTree *t, cudaStream_t st, bool recount)
     const int slots = launch_nodes(t);
     const int grid = std::max(1, std::min(div_up(slots, 256), 8 * device_props().num_sms));
     if (recount) {
-        NB_TRY(t->nkids.reserve(sizeof(int) * (size_t)slots));
         NB_TRY(t->kbase.reserve(sizeof(int) * ((size_t)slots + 1)));
         int *next = t->kbase.as<int>() + slots;  // the group counter (group 0: the root)
         NB_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(int), st));
-        count_kids_kernel<<<grid, 256, 0, st>>>(t->nodes.as<BHNode>(), d_total(t),
-                                                t->nkids.as<int>(), t->kbase.as<int>(), next);
+        alloc_groups_kernel<<<grid, 256, 0, st>>>(t->occ.as<unsigned>(), d_total(t),
+                                                  t->kbase.as<int>(), next);
         NB_LAUNCH_CHECK();
     }
     NB_TRY(t->gnodes.reserve(sizeof(BHGNode) * (size_t)slots));
     NB_TRY(t->gnk.reserve((size_t)slots));
-    NB_TRY(t->gpcen.reserve(sizeof(float4) * (size_t)slots));
+    if (t->ref_open) NB_TRY(t->gpcen.reserve(sizeof(float4) * (size_t)slots));
     if (t->with_quad) NB_TRY(t->gquad.reserve(sizeof(float4) * 2 * (size_t)slots));
     group_kernel<<<grid, 256, 0, st>>>(
-        t->nodes.as<BHNode>(), d_total(t), t->nkids.as<int>(), t->kbase.as<int>(),
-        t->pcen.as<float4>(), t->with_quad ? t->quad.as<float4>() : nullptr,
-        t->gnodes.as<BHGNode>(), t->gnk.as<unsigned char>(), t->gpcen.as<float4>(),
+        t->nodes.as<BHNode>(), d_total(t), t->occ.as<unsigned>(), t->kbase.as<int>(),
+        t->parent.as<int>(), t->octant.as<unsigned char>(),
+        t->ref_open ? t->pcen.as<float4>() : nullptr,
+        t->with_quad ? t->quad.as<float4>() : nullptr, t->gnodes.as<BHGNode>(),
+        t->gnk.as<unsigned char>(), t->gpcen.as<float4>(),
         t->with_quad ? t->gquad.as<float4>() : nullptr);
     NB_LAUNCH_CHECK();
     return NB_OK;
@@ -1725,6 +1786,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     if (ax && reuse > 1 && t->tree_valid && t->n == n && t->evals_since_build < reuse) {
         NB_TRY(refit(t, x, y, z, m, n, st));
         if (quad) NB_TRY(compute_quads(t, x, y, z, m, n, st));
+        NB_TRY(ensure_pcen(t, st));
         NB_TRY(group_nodes(t, st, false));
         ++t->evals_since_build;
         return launch_walk(t, n, G, eps2, theta, ax, ay, az, st, timer);
@@ -1738,6 +1800,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     NB_TRY(t->chain_len.reserve(sizeof(int) * N));
     NB_TRY(t->chain_depth.reserve(sizeof(int) * N));
     NB_TRY(t->offsets.reserve(sizeof(int) * (N + 1)));
+    NB_TRY(t->pstart.reserve(sizeof(int) * N));
     if (!t->stats.ptr) {
         NB_TRY(t->stats.reserve(sizeof(BHStats)));
         NB_CUDA_TRY(cudaMemsetAsync(t->stats.ptr, 0, sizeof(BHStats), st));
@@ -1754,7 +1817,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     NB_TRY(scan_exclusive<D4>(t->moments.as<D4>(), n, t->prefix.as<D4>(), t->scan_tmp, st));
     chain_kernel<<<div_up(n, 256), 256, 0, st>>>(kin, n, leaf_capacity, root,
                                                  t->chain_len.as<int>(),
-                                                 t->chain_depth.as<int>());
+                                                 t->chain_depth.as<int>(), t->pstart.as<int>());
     NB_LAUNCH_CHECK();
     NB_TRY(scan_exclusive<int>(t->chain_len.as<int>(), n, t->offsets.as<int>(), t->scan_tmp,
                                st));
@@ -1764,7 +1827,9 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     const size_t cap = node_bound(n, leaf_capacity);
     NB_TRY(t->nodes.reserve(sizeof(BHNode) * cap));
     NB_TRY(t->node_depth.reserve(cap));
-    NB_TRY(t->pcen.reserve(sizeof(float4) * cap));
+    NB_TRY(t->parent.reserve(sizeof(int) * cap));
+    NB_TRY(t->octant.reserve(cap));
+    NB_TRY(t->occ.reserve(sizeof(unsigned) * cap));
     if (!t->h_total) NB_CUDA_TRY(cudaMallocHost(&t->h_total, sizeof(int)));
     if (!t->total_ready) NB_CUDA_TRY(cudaEventCreateWithFlags(&t->total_ready,
                                                               cudaEventDisableTiming));
@@ -1782,14 +1847,19 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     t->num_nodes = -1;
     t->n = n;
     NB_CUDA_TRY(cudaMemsetAsync(stats, 0, offsetof(BHStats, total), st));
+    NB_CUDA_TRY(cudaMemsetAsync(t->occ.ptr, 0, sizeof(unsigned) * cap, st));
     node_kernel<<<div_up(n, 256), 256, 0, st>>>(kin, n, leaf_capacity, root,
                                                 t->chain_len.as<int>(), t->chain_depth.as<int>(),
                                                 t->offsets.as<int>(), t->prefix.as<D4>(),
                                                 t->nodes.as<BHNode>(),
                                                 t->node_depth.as<unsigned char>(),
-                                                t->pcen.as<float4>(), stats, t->node_cap);
+                                                t->pstart.as<int>(), t->parent.as<int>(),
+                                                t->octant.as<unsigned char>(),
+                                                t->occ.as<unsigned>(), stats, t->node_cap);
     NB_LAUNCH_CHECK();
     if (quad) NB_TRY(compute_quads(t, x, y, z, m, n, st));
+    t->pcen_valid = false;
+    NB_TRY(ensure_pcen(t, st));
     NB_TRY(group_nodes(t, st, true));
     t->tree_valid = true;
     t->evals_since_build = 0;
