@@ -1,6 +1,6 @@
 // nb_bh.cu -- Barnes-Hut on sm_103a: 63-bit Morton encode, LSD radix sort,
 // a parallel octree build read off the sorted codes, monopoles from FP64 prefix
-// sums, and a stackless warp-cooperative walk.
+// sums, and a warp-cooperative walk over child groups.
 //
 // Replaces BarnesHutForceCalculator (CUDA/src/force_calculator_barnes_hut.cu):
 // six CUB min/max passes (:108-173), a 30-bit Morton code (:217-251), a CUB pair
@@ -30,15 +30,17 @@
 // from FP64 prefix sums of (m, m x, m y, m z) over the sorted bodies (positions
 // relative to the root centre), so no level-by-level pass is needed.
 //
-// Walk.  One warp walks for 32 consecutive sorted bodies.  At each node every
-// lane applies the reference's opening test (open when size^2 >= theta^2 d^2 to
-// the COM, or when the node holds the lane's own body); the warp opens the node
-// if any lane does (so each body gets a refinement of its own walk, never a
-// coarser one), descending to node+1 or, for a leaf, summing its bodies; a node
-// no lane opens is a monopole for all lanes and the walk jumps to its skip
-// pointer.  Node indices only grow, so the walk ends after at most
-// num_nodes steps: there is no stack to overflow.  Accelerations are scattered
-// back to the original order in FP64, multiplied by G.
+// Walk.  One warp walks for 64 consecutive sorted bodies, two per lane.  At
+// each node every body applies the reference's opening test (open when size^2
+// >= theta^2 d^2 to the COM, or when the node holds the body); the warp opens
+// the node if any body does (so each body gets a refinement of its own walk,
+// never a coarser one).  The children of every node are stored together (a
+// group): the warp reads a group in one round trip, adds the monopoles of the
+// children no body opens and the bodies of opened leaves, and pushes the
+// groups of opened internal children on its stack, which holds the deepest
+// tree's groups.  The stackless preorder walk over skip pointers finds the
+// same interactions (NB_BH_WALK=preorder).  Accelerations are scattered back
+// to the original order in FP64, multiplied by G.
 #include "nb_internal.h"
 #include "nb_check.cuh"
 #include "nb_curve.cuh"
