@@ -415,9 +415,11 @@ exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
 
     // the lane's i-bodies' box, for the per-lane test of a chunk
     float lmn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, lmx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+    bool ival[IPT];
 #pragma unroll
-    for (int k = 0; k < IPT; ++k)
-        if ((tile0 + k) * kChunk + lane < n) {
+    for (int k = 0; k < IPT; ++k) {
+        ival[k] = (tile0 + k) * kChunk + lane < n;
+        if (ival[k]) {
             const float q[3] = {-nsx[k].x, -nsy[k].x, -nsz[k].x};
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
@@ -425,10 +427,11 @@ exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                 lmx[a] = fmaxf(lmx[a], q[a]);
             }
         }
-    // The test below only skips work, so it must never skip a chunk that holds
-    // a left-out pair: R grows by a slack far above the FP32 roundings that
-    // separate the boxes (hi coordinates) from the staged ones and the box
-    // distance from the pair's r^2 (softening included).
+    }
+    // The tests below only skip work, so they must never skip a chunk (or an
+    // i-chunk of it) that holds a left-out pair: R grows by a slack far above
+    // the FP32 roundings that separate the boxes (hi coordinates) from the
+    // staged ones and the box distance from the pair's r^2 (softening included).
     const float Rw = sqrtf(gm.thr2x);
     const float cmag = fmaxf(fabsf(gm.c[0]), fmaxf(fabsf(gm.c[1]), fabsf(gm.c[2])));
     const float e2slack = 1e-6f * (gm.thr2x + eps2);
@@ -479,6 +482,28 @@ exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
         }
         if (jc < 0) break;
 
+        // the i-chunks with a body within R of the chunk's box (a lane's own
+        // body against the box, the same slack)
+        bool need[IPT];
+        {
+            const float4 jmn = box[2 * jc], jmx = box[2 * jc + 1];
+            const float bx0 = jmn.x - gm.c[0], by0 = jmn.y - gm.c[1], bz0 = jmn.z - gm.c[2];
+            const float bx1 = jmx.x - gm.c[0], by1 = jmx.y - gm.c[1], bz1 = jmx.z - gm.c[2];
+            const float mag = cmag + fmaxf(fmaxf(fabsf(bx0), fabsf(bx1)),
+                                           fmaxf(fmaxf(fabsf(by0), fabsf(by1)),
+                                                 fmaxf(fabsf(bz0), fabsf(bz1))));
+            const float Re = Rw + 1e-6f * mag;
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const float px = -nsx[k].x, py = -nsy[k].x, pz = -nsz[k].x;
+                const float gx = fmaxf(0.f, fmaxf(bx0 - px, px - bx1));
+                const float gy = fmaxf(0.f, fmaxf(by0 - py, py - by1));
+                const float gz = fmaxf(0.f, fmaxf(bz0 - pz, pz - bz1));
+                need[k] = __any_sync(0xffffffffu,
+                                     ival[k] && gx * gx + gy * gy + gz * gz <= Re * Re + e2slack);
+            }
+        }
+
         // stage the chunk as the main kernel's near path does
         const int b = jc * kChunk + lane;
         float Sx = 1.0e18f, Sy = 1.0e18f, Sz = 1.0e18f, Ex = 0.f, Ey = 0.f, Ez = 0.f, mj = 0.f,
@@ -499,15 +524,15 @@ exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
         // the left-out pairs: the main kernel's r^2 test, same operands
         uint32_t mk[IPT];
 #pragma unroll
-        for (int k = 0; k < IPT; ++k) mk[k] = 0u;
+        for (int k = 0; k < IPT; ++k) {
+            mk[k] = 0u;
+            if (!need[k]) continue;
+            const int i = (tile0 + k) * kChunk + lane;
 #pragma unroll 2
-        for (int p = 0; p < kChunk / 2; ++p) {
-            const JPair j = pair_tile_get(sg, p);
-            const int j0 = jc * kChunk + 2 * p;
-#pragma unroll
-            for (int k = 0; k < IPT; ++k) {
+            for (int p = 0; p < kChunk / 2; ++p) {
+                const JPair j = pair_tile_get(sg, p);
+                const int j0 = jc * kChunk + 2 * p;
                 const PairGeom g = pair_geom(j, nsx[k], nsy[k], nsz[k], nex[k], ney[k], nez[k], e2);
-                const int i = (tile0 + k) * kChunk + lane;
                 const uint32_t b0 = (g.r2.x < thrx && i < n && j0 != i) ? 1u : 0u;
                 const uint32_t b1 = (g.r2.y < thrx && i < n && j0 + 1 != i) ? 2u : 0u;
                 mk[k] |= (b0 | b1) << (2 * p);
