@@ -638,6 +638,8 @@ __global__ void combine_sorted_kernel(const float *__restrict__ psum,
     if (i >= n) return;
     const size_t plane = (size_t)n;
     float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
+    // the loads of several segments go out before their (ordered) sums
+#pragma unroll 8
     for (int s = 0; s < segments; ++s) {
         const size_t base = (size_t)s * 3 * plane;
 #pragma unroll
