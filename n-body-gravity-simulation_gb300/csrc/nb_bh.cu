@@ -580,6 +580,29 @@ scan_apply_kernel(const T *__restrict__ in, int n, const T *__restrict__ block_o
     }
 }
 
+// Exclusive scan of at most kSmallScanMax ints by one block of 1024 threads
+// (the radix sort's digit counts, one scan per pass: one launch instead of
+// three): each thread sums a contiguous run, a block scan numbers the runs and
+// each thread writes its run's prefixes.  out has len + 1 entries.
+constexpr int kSmallScanMax = 1024 * 32;
+__global__ void __launch_bounds__(1024)
+scan_small_kernel(const int *__restrict__ in, int len, int *__restrict__ out)
+{
+    __shared__ int warp_sums[33];
+    const int per = (len + 1023) / 1024;
+    const int b = threadIdx.x * per, e = min(len, b + per);
+    int s = 0;
+    for (int k = b; k < e; ++k) s += in[k];
+    int total;
+    int run = block_exclusive<int, 32>(s, warp_sums, &total);
+    for (int k = b; k < e; ++k) {
+        const int v = in[k];
+        out[k] = run;
+        run += v;
+    }
+    if (threadIdx.x == 0) out[len] = total;
+}
+
 // ------------------------------------------------------------ tree build
 // First index after i whose depth-d prefix differs from code[i]'s (galloping).
 __device__ __forceinline__ int cell_end(const uint64_t *__restrict__ c, int n, int i, int d)
@@ -1408,6 +1431,18 @@ nb_status scan_exclusive(const T *in, int n, T *out, DevBuf &tmp, cudaStream_t s
     return NB_OK;
 }
 
+// An exclusive int scan: one block up to kSmallScanMax entries, else three
+// passes.
+nb_status scan_ints(const int *in, int n, int *out, DevBuf &tmp, cudaStream_t st)
+{
+    if (n <= kSmallScanMax) {
+        scan_small_kernel<<<1, 1024, 0, st>>>(in, n, out);
+        NB_LAUNCH_CHECK();
+        return NB_OK;
+    }
+    return scan_exclusive<int>(in, n, out, tmp, st);
+}
+
 } // namespace
 
 struct BHTree {
@@ -1517,7 +1552,7 @@ static nb_status radix_passes(BHTree *t, int n, int first_shift, cudaStream_t st
     for (int shift = first_shift; shift < 64; shift += 8) {
         radix_hist_kernel<<<num_tiles, 256, 0, st>>>(kin, n, shift, counts, num_tiles);
         NB_LAUNCH_CHECK();
-        NB_TRY(scan_exclusive<int>(counts, 256 * num_tiles, digit_off, t->scan_tmp, st));
+        NB_TRY(scan_ints(counts, 256 * num_tiles, digit_off, t->scan_tmp, st));
         radix_scatter_kernel<<<num_tiles, 256, 0, st>>>(kin, vin, kout, vout, n, shift,
                                                         digit_off, num_tiles);
         NB_LAUNCH_CHECK();
@@ -1821,7 +1856,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
                                                  t->chain_len.as<int>(),
                                                  t->chain_depth.as<int>(), t->pstart.as<int>());
     NB_LAUNCH_CHECK();
-    NB_TRY(scan_exclusive<int>(t->chain_len.as<int>(), n, t->offsets.as<int>(), t->scan_tmp,
+    NB_TRY(scan_ints(t->chain_len.as<int>(), n, t->offsets.as<int>(), t->scan_tmp,
                                st));
     // No host read of the node count before the walk: node storage is sized
     // for the bound, the kernels read the count on the device, and the count
