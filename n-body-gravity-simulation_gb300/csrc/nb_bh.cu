@@ -302,152 +302,6 @@ hilbert_kernel(const double *__restrict__ x, const double *__restrict__ y,
     vals[i] = (uint32_t)i;
 }
 
-// ------------------------------------------------------------ radix sort
-constexpr int kSortWarps = 8;
-constexpr int kSortRounds = 8;
-constexpr int kSortTile = kSortWarps * 32 * kSortRounds;  // 2048 keys
-
-__global__ void __launch_bounds__(256)
-radix_hist_kernel(const uint64_t *__restrict__ keys, int n, int shift, int *__restrict__ counts,
-                  int num_tiles)
-{
-    __shared__ int h[kSortWarps][256];
-    const int warp = threadIdx.x >> 5;
-    for (int k = threadIdx.x; k < kSortWarps * 256; k += 256) (&h[0][0])[k] = 0;
-    __syncthreads();
-    const int base = blockIdx.x * kSortTile;
-    for (int k = threadIdx.x; k < kSortTile; k += 256) {
-        const int idx = base + k;
-        if (idx < n) atomicAdd(&h[warp][(int)((keys[idx] >> shift) & 0xFF)], 1);
-    }
-    __syncthreads();
-    int c = 0;
-    for (int w = 0; w < kSortWarps; ++w) c += h[w][threadIdx.x];
-    counts[threadIdx.x * num_tiles + blockIdx.x] = c;
-}
-
-// Stable scatter of one 8-bit digit.  Warp w of the block ranks keys
-// [tile + w*256, +256) in rounds of 32 (lane order), so ranks follow the input
-// order; per-warp digit counts are turned into per-warp offsets.  The tile is
-// then put in digit order in shared memory and written out by consecutive
-// threads, so each digit's run of the tile goes to consecutive addresses (the
-// tile's global offset per digit comes from the scanned histogram).
-__global__ void __launch_bounds__(256)
-radix_scatter_kernel(const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin,
-                     uint64_t *__restrict__ kout, uint32_t *__restrict__ vout, int n, int shift,
-                     const int *__restrict__ offsets, int num_tiles)
-{
-    __shared__ int wh[kSortWarps][256];
-    __shared__ int toff[256];    // global position of the tile's first key of digit d
-    __shared__ int tstart[256];  // position in the tile of its first key of digit d
-    __shared__ int wsum[kSortWarps];
-    __shared__ uint64_t skey[kSortTile];
-    __shared__ uint32_t sval[kSortTile];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k = threadIdx.x; k < kSortWarps * 256; k += 256) (&wh[0][0])[k] = 0;
-    toff[threadIdx.x] = offsets[threadIdx.x * num_tiles + blockIdx.x];
-    __syncthreads();
-    const int tile0 = blockIdx.x * kSortTile;
-    const int base = tile0 + warp * 32 * kSortRounds;
-    uint64_t key[kSortRounds];
-    uint32_t val[kSortRounds];
-    int rank[kSortRounds], dig[kSortRounds];
-#pragma unroll
-    for (int r = 0; r < kSortRounds; ++r) {
-        const int idx = base + r * 32 + lane;
-        const bool valid = idx < n;
-        key[r] = valid ? kin[idx] : 0ull;
-        val[r] = valid ? vin[idx] : 0u;
-        const int d = valid ? (int)((key[r] >> shift) & 0xFF) : -1;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        const int before = __popc(peers & ((1u << lane) - 1u));
-        const int leader = 31 - __clz(peers);
-        const int b = valid ? wh[warp][d] : 0;
-        __syncwarp();
-        if (valid && lane == leader) wh[warp][d] = b + __popc(peers);
-        __syncwarp();
-        rank[r] = b + before;
-        dig[r] = d;
-    }
-    __syncthreads();
-    {
-        // per-warp offsets within the digit, and the tile's digit starts
-        // (exclusive scan of the digit totals: warp shuffles, then warp sums)
-        const int d = threadIdx.x;
-        int run = 0;
-        for (int w = 0; w < kSortWarps; ++w) {
-            const int c = wh[w][d];
-            wh[w][d] = run;
-            run += c;
-        }
-        int inc = run;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += u;
-        }
-        if (lane == 31) wsum[warp] = inc;
-        __syncthreads();
-        int before = 0;
-        for (int w = 0; w < warp; ++w) before += wsum[w];
-        tstart[d] = before + inc - run;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < kSortRounds; ++r) {
-        const int d = dig[r];
-        if (d >= 0) {
-            const int lpos = tstart[d] + wh[warp][d] + rank[r];
-            skey[lpos] = key[r];
-            sval[lpos] = val[r];
-        }
-    }
-    __syncthreads();
-    const int count = min(kSortTile, n - tile0);
-    for (int j = threadIdx.x; j < count; j += 256) {
-        const uint64_t k = skey[j];
-        const int d = (int)((k >> shift) & 0xFF);
-        const int pos = toff[d] + (j - tstart[d]);
-        if (!NB_IN_RANGE(pos, n)) continue;
-        kout[pos] = k;
-        vout[pos] = sval[j];
-    }
-}
-
-// ------------------------------------------------------------ gather
-__global__ void __launch_bounds__(256)
-gather_kernel(const uint32_t *__restrict__ order, const double *__restrict__ x,
-              const double *__restrict__ y, const double *__restrict__ z,
-              const double *__restrict__ m, int n, const BHRoot *__restrict__ root,
-              float4 *__restrict__ body, D4 *__restrict__ moments)
-{
-    const int i = blockIdx.x * 256 + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t o = order[i];
-    if (!NB_IN_RANGE(o, n)) return;
-    const double rx = x[o] - root->cx, ry = y[o] - root->cy, rz = z[o] - root->cz;
-    const double mm = m[o];
-    body[i] = make_float4((float)rx, (float)ry, (float)rz, (float)mm);
-    moments[i] = D4{mm, mm * rx, mm * ry, mm * rz};
-}
-
-// Second moments m x x^T (relative to the root centre) of every sorted body,
-// for the quadrupoles: a = (m x x, m y y, m z z, m x y), b = (m x z, m y z, 0, 0).
-__global__ void __launch_bounds__(256)
-gather2_kernel(const uint32_t *__restrict__ order, const double *__restrict__ x,
-               const double *__restrict__ y, const double *__restrict__ z,
-               const double *__restrict__ m, int n, const BHRoot *__restrict__ root,
-               D4 *__restrict__ ma, D4 *__restrict__ mb)
-{
-    const int i = blockIdx.x * 256 + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t o = order[i];
-    const double rx = x[o] - root->cx, ry = y[o] - root->cy, rz = z[o] - root->cz;
-    const double mm = m[o];
-    ma[i] = D4{mm * rx * rx, mm * ry * ry, mm * rz * rz, mm * rx * ry};
-    mb[i] = D4{mm * rx * rz, mm * ry * rz, 0.0, 0.0};
-}
-
 // ------------------------------------------------------------ scans (fixed order)
 template <class T> struct Add;
 template <> struct Add<int> {
@@ -580,27 +434,169 @@ scan_apply_kernel(const T *__restrict__ in, int n, const T *__restrict__ block_o
     }
 }
 
-// Exclusive scan of at most kSmallScanMax ints by one block of 1024 threads
-// (the radix sort's digit counts, one scan per pass: one launch instead of
-// three): each thread sums a contiguous run, a block scan numbers the runs and
-// each thread writes its run's prefixes.  out has len + 1 entries.
-constexpr int kSmallScanMax = 1024 * 32;
-__global__ void __launch_bounds__(1024)
-scan_small_kernel(const int *__restrict__ in, int len, int *__restrict__ out)
+// ------------------------------------------------------------ radix sort
+constexpr int kSortWarps = 8;
+constexpr int kSortRounds = 8;
+constexpr int kSortTile = kSortWarps * 32 * kSortRounds;  // 2048 keys
+// Up to this many tiles (n <= 262,144) a scatter block sums the per-tile digit
+// counts itself instead of a separate scan pass.
+constexpr int kSortDirectTiles = 128;
+
+__global__ void __launch_bounds__(256)
+radix_hist_kernel(const uint64_t *__restrict__ keys, int n, int shift, int *__restrict__ counts,
+                  int num_tiles)
 {
-    __shared__ int warp_sums[33];
-    const int per = (len + 1023) / 1024;
-    const int b = threadIdx.x * per, e = min(len, b + per);
-    int s = 0;
-    for (int k = b; k < e; ++k) s += in[k];
-    int total;
-    int run = block_exclusive<int, 32>(s, warp_sums, &total);
-    for (int k = b; k < e; ++k) {
-        const int v = in[k];
-        out[k] = run;
-        run += v;
+    __shared__ int h[kSortWarps][256];
+    const int warp = threadIdx.x >> 5;
+    for (int k = threadIdx.x; k < kSortWarps * 256; k += 256) (&h[0][0])[k] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile;
+    for (int k = threadIdx.x; k < kSortTile; k += 256) {
+        const int idx = base + k;
+        if (idx < n) atomicAdd(&h[warp][(int)((keys[idx] >> shift) & 0xFF)], 1);
     }
-    if (threadIdx.x == 0) out[len] = total;
+    __syncthreads();
+    int c = 0;
+    for (int w = 0; w < kSortWarps; ++w) c += h[w][threadIdx.x];
+    counts[threadIdx.x * num_tiles + blockIdx.x] = c;
+}
+
+// Stable scatter of one 8-bit digit.  Warp w of the block ranks keys
+// [tile + w*256, +256) in rounds of 32 (lane order), so ranks follow the input
+// order; per-warp digit counts are turned into per-warp offsets.  The tile is
+// then put in digit order in shared memory and written out by consecutive
+// threads, so each digit's run of the tile goes to consecutive addresses.  The
+// tile's global offset per digit comes from the scanned histogram (offsets),
+// or, when offsets is null (few tiles), from the per-tile counts directly:
+// the digit's count in the earlier tiles plus all keys of smaller digits.
+__global__ void __launch_bounds__(256)
+radix_scatter_kernel(const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin,
+                     uint64_t *__restrict__ kout, uint32_t *__restrict__ vout, int n, int shift,
+                     const int *__restrict__ offsets, const int *__restrict__ counts,
+                     int num_tiles)
+{
+    __shared__ int wh[kSortWarps][256];
+    __shared__ int toff[256];    // global position of the tile's first key of digit d
+    __shared__ int tstart[256];  // position in the tile of its first key of digit d
+    __shared__ int wsum[kSortWarps];
+    __shared__ int dsum[kSortWarps + 1];
+    __shared__ uint64_t skey[kSortTile];
+    __shared__ uint32_t sval[kSortTile];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k < kSortWarps * 256; k += 256) (&wh[0][0])[k] = 0;
+    if (offsets) {
+        toff[threadIdx.x] = offsets[threadIdx.x * num_tiles + blockIdx.x];
+    } else {
+        const int *row = counts + threadIdx.x * num_tiles;
+        int before = 0, all = 0;
+        for (int tl = 0; tl < num_tiles; ++tl) {
+            const int c = row[tl];
+            all += c;
+            if (tl < (int)blockIdx.x) before += c;
+        }
+        int keys;
+        toff[threadIdx.x] = block_exclusive<int, kSortWarps>(all, dsum, &keys) + before;
+    }
+    __syncthreads();
+    const int tile0 = blockIdx.x * kSortTile;
+    const int base = tile0 + warp * 32 * kSortRounds;
+    uint64_t key[kSortRounds];
+    uint32_t val[kSortRounds];
+    int rank[kSortRounds], dig[kSortRounds];
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r) {
+        const int idx = base + r * 32 + lane;
+        const bool valid = idx < n;
+        key[r] = valid ? kin[idx] : 0ull;
+        val[r] = valid ? vin[idx] : 0u;
+        const int d = valid ? (int)((key[r] >> shift) & 0xFF) : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int before = __popc(peers & ((1u << lane) - 1u));
+        const int leader = 31 - __clz(peers);
+        const int b = valid ? wh[warp][d] : 0;
+        __syncwarp();
+        if (valid && lane == leader) wh[warp][d] = b + __popc(peers);
+        __syncwarp();
+        rank[r] = b + before;
+        dig[r] = d;
+    }
+    __syncthreads();
+    {
+        // per-warp offsets within the digit, and the tile's digit starts
+        // (exclusive scan of the digit totals: warp shuffles, then warp sums)
+        const int d = threadIdx.x;
+        int run = 0;
+        for (int w = 0; w < kSortWarps; ++w) {
+            const int c = wh[w][d];
+            wh[w][d] = run;
+            run += c;
+        }
+        int inc = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += u;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        int before = 0;
+        for (int w = 0; w < warp; ++w) before += wsum[w];
+        tstart[d] = before + inc - run;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r) {
+        const int d = dig[r];
+        if (d >= 0) {
+            const int lpos = tstart[d] + wh[warp][d] + rank[r];
+            skey[lpos] = key[r];
+            sval[lpos] = val[r];
+        }
+    }
+    __syncthreads();
+    const int count = min(kSortTile, n - tile0);
+    for (int j = threadIdx.x; j < count; j += 256) {
+        const uint64_t k = skey[j];
+        const int d = (int)((k >> shift) & 0xFF);
+        const int pos = toff[d] + (j - tstart[d]);
+        if (!NB_IN_RANGE(pos, n)) continue;
+        kout[pos] = k;
+        vout[pos] = sval[j];
+    }
+}
+
+// ------------------------------------------------------------ gather
+__global__ void __launch_bounds__(256)
+gather_kernel(const uint32_t *__restrict__ order, const double *__restrict__ x,
+              const double *__restrict__ y, const double *__restrict__ z,
+              const double *__restrict__ m, int n, const BHRoot *__restrict__ root,
+              float4 *__restrict__ body, D4 *__restrict__ moments)
+{
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = order[i];
+    if (!NB_IN_RANGE(o, n)) return;
+    const double rx = x[o] - root->cx, ry = y[o] - root->cy, rz = z[o] - root->cz;
+    const double mm = m[o];
+    body[i] = make_float4((float)rx, (float)ry, (float)rz, (float)mm);
+    moments[i] = D4{mm, mm * rx, mm * ry, mm * rz};
+}
+
+// Second moments m x x^T (relative to the root centre) of every sorted body,
+// for the quadrupoles: a = (m x x, m y y, m z z, m x y), b = (m x z, m y z, 0, 0).
+__global__ void __launch_bounds__(256)
+gather2_kernel(const uint32_t *__restrict__ order, const double *__restrict__ x,
+               const double *__restrict__ y, const double *__restrict__ z,
+               const double *__restrict__ m, int n, const BHRoot *__restrict__ root,
+               D4 *__restrict__ ma, D4 *__restrict__ mb)
+{
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = order[i];
+    const double rx = x[o] - root->cx, ry = y[o] - root->cy, rz = z[o] - root->cz;
+    const double mm = m[o];
+    ma[i] = D4{mm * rx * rx, mm * ry * ry, mm * rz * rz, mm * rx * ry};
+    mb[i] = D4{mm * rx * rz, mm * ry * rz, 0.0, 0.0};
 }
 
 // ------------------------------------------------------------ tree build
@@ -1431,18 +1427,6 @@ nb_status scan_exclusive(const T *in, int n, T *out, DevBuf &tmp, cudaStream_t s
     return NB_OK;
 }
 
-// An exclusive int scan: one block up to kSmallScanMax entries, else three
-// passes.
-nb_status scan_ints(const int *in, int n, int *out, DevBuf &tmp, cudaStream_t st)
-{
-    if (n <= kSmallScanMax) {
-        scan_small_kernel<<<1, 1024, 0, st>>>(in, n, out);
-        NB_LAUNCH_CHECK();
-        return NB_OK;
-    }
-    return scan_exclusive<int>(in, n, out, tmp, st);
-}
-
 } // namespace
 
 struct BHTree {
@@ -1552,9 +1536,11 @@ static nb_status radix_passes(BHTree *t, int n, int first_shift, cudaStream_t st
     for (int shift = first_shift; shift < 64; shift += 8) {
         radix_hist_kernel<<<num_tiles, 256, 0, st>>>(kin, n, shift, counts, num_tiles);
         NB_LAUNCH_CHECK();
-        NB_TRY(scan_ints(counts, 256 * num_tiles, digit_off, t->scan_tmp, st));
+        const bool direct = num_tiles <= kSortDirectTiles;  // offsets from the counts
+        if (!direct) NB_TRY(scan_exclusive<int>(counts, 256 * num_tiles, digit_off, t->scan_tmp, st));
         radix_scatter_kernel<<<num_tiles, 256, 0, st>>>(kin, vin, kout, vout, n, shift,
-                                                        digit_off, num_tiles);
+                                                        direct ? nullptr : digit_off, counts,
+                                                        num_tiles);
         NB_LAUNCH_CHECK();
         std::swap(kin, kout);
         std::swap(vin, vout);
@@ -1856,7 +1842,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
                                                  t->chain_len.as<int>(),
                                                  t->chain_depth.as<int>(), t->pstart.as<int>());
     NB_LAUNCH_CHECK();
-    NB_TRY(scan_ints(t->chain_len.as<int>(), n, t->offsets.as<int>(), t->scan_tmp,
+    NB_TRY(scan_exclusive<int>(t->chain_len.as<int>(), n, t->offsets.as<int>(), t->scan_tmp,
                                st));
     // No host read of the node count before the walk: node storage is sized
     // for the bound, the kernels read the count on the device, and the count
