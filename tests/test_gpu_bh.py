@@ -74,7 +74,11 @@ def check_preorder(nodes):
             assert skip[v] == v + 1
 
 
-WORKLOADS = ["cube5000", "plummer20000", "diskbulge20000", "cube_leaf1_3000", "clustered"]
+# diskbulge200000: ~98 sort tiles, where each scatter block sums the per-tile
+# digit counts itself (the scanned offsets take over above 128 tiles, covered by
+# the configuration-size test)
+WORKLOADS = ["cube5000", "plummer20000", "diskbulge20000", "diskbulge200000", "cube_leaf1_3000",
+             "clustered"]
 
 
 def make(nb, oracle, name):
@@ -84,6 +88,8 @@ def make(nb, oracle, name):
         return nb.plummer(20000, seed=3), 8
     if name == "diskbulge20000":
         return nb.disk_bulge(20000, seed=4), 8
+    if name == "diskbulge200000":
+        return nb.disk_bulge(200000, seed=14), 8
     if name == "cube_leaf1_3000":
         return cube(oracle, 3000, seed=7), 1
     # two tight clumps plus duplicates: deep chains and unsplittable cells
