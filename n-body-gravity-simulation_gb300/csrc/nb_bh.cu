@@ -441,6 +441,10 @@ constexpr int kSortTile = kSortWarps * 32 * kSortRounds;  // 2048 keys
 // Up to this many tiles (n <= 262,144) a scatter block sums the per-tile digit
 // counts itself instead of a separate scan pass.
 constexpr int kSortDirectTiles = 128;
+// Up to this many tiles (n <= 131,072) the scatter also counts the next pass's
+// digits (a global atomic per key), so passes after the first need no
+// histogram launch; above it the atomics cost more than the launch saves.
+constexpr int kSortFusedTiles = 64;
 
 __global__ void __launch_bounds__(256)
 radix_hist_kernel(const uint64_t *__restrict__ keys, int n, int shift, int *__restrict__ counts,
@@ -469,11 +473,15 @@ radix_hist_kernel(const uint64_t *__restrict__ keys, int n, int shift, int *__re
 // tile's global offset per digit comes from the scanned histogram (offsets),
 // or, when offsets is null (few tiles), from the per-tile counts directly:
 // the digit's count in the earlier tiles plus all keys of smaller digits.
+// next_counts (not for the last pass) receives the next pass's per-tile
+// histogram, counted as the keys land (integer adds: any order gives the same
+// counts), so that pass needs no histogram launch; each block also clears its
+// column of zero_counts, the buffer the pass after next counts into.
 __global__ void __launch_bounds__(256)
 radix_scatter_kernel(const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin,
                      uint64_t *__restrict__ kout, uint32_t *__restrict__ vout, int n, int shift,
                      const int *__restrict__ offsets, const int *__restrict__ counts,
-                     int num_tiles)
+                     int *__restrict__ next_counts, int *__restrict__ zero_counts, int num_tiles)
 {
     __shared__ int wh[kSortWarps][256];
     __shared__ int toff[256];    // global position of the tile's first key of digit d
@@ -562,7 +570,10 @@ radix_scatter_kernel(const uint64_t *__restrict__ kin, const uint32_t *__restric
         if (!NB_IN_RANGE(pos, n)) continue;
         kout[pos] = k;
         vout[pos] = sval[j];
+        if (next_counts)
+            atomicAdd(&next_counts[(int)((k >> (shift + 8)) & 0xFF) * num_tiles + pos / kSortTile], 1);
     }
+    if (zero_counts) zero_counts[threadIdx.x * num_tiles + blockIdx.x] = 0;
 }
 
 // ------------------------------------------------------------ gather
@@ -1519,8 +1530,9 @@ static nb_status reserve_sort(BHTree *t, int n)
     NB_TRY(t->keys1.reserve(sizeof(uint64_t) * N));
     NB_TRY(t->vals0.reserve(sizeof(uint32_t) * N));
     NB_TRY(t->vals1.reserve(sizeof(uint32_t) * N));
-    // digit counts per tile, then their exclusive scan (256 * tiles + 1 each)
-    NB_TRY(t->hist.reserve(sizeof(int) * 2 * (256 * (size_t)num_tiles + 1)));
+    // three rotating digit-count buffers per tile, then their exclusive scan
+    // (256 * tiles + 1 each)
+    NB_TRY(t->hist.reserve(sizeof(int) * 4 * (256 * (size_t)num_tiles + 1)));
     return NB_OK;
 }
 
@@ -1531,16 +1543,27 @@ static nb_status radix_passes(BHTree *t, int n, int first_shift, cudaStream_t st
     const int num_tiles = div_up(n, kSortTile);
     uint64_t *kin = t->keys0.as<uint64_t>(), *kout = t->keys1.as<uint64_t>();
     uint32_t *vin = t->vals0.as<uint32_t>(), *vout = t->vals1.as<uint32_t>();
-    int *counts = t->hist.as<int>();
-    int *digit_off = counts + 256 * (size_t)num_tiles + 1;
-    for (int shift = first_shift; shift < 64; shift += 8) {
-        radix_hist_kernel<<<num_tiles, 256, 0, st>>>(kin, n, shift, counts, num_tiles);
-        NB_LAUNCH_CHECK();
-        const bool direct = num_tiles <= kSortDirectTiles;  // offsets from the counts
-        if (!direct) NB_TRY(scan_exclusive<int>(counts, 256 * num_tiles, digit_off, t->scan_tmp, st));
-        radix_scatter_kernel<<<num_tiles, 256, 0, st>>>(kin, vin, kout, vout, n, shift,
-                                                        direct ? nullptr : digit_off, counts,
-                                                        num_tiles);
+    // pass p reads counts cnt[p % 3], counts the next digit into cnt[(p + 1) % 3]
+    // and clears cnt[(p + 2) % 3] (read by pass p - 1) for pass p + 1
+    const size_t stride = 256 * (size_t)num_tiles + 1;
+    int *cnt[3] = {t->hist.as<int>(), t->hist.as<int>() + stride, t->hist.as<int>() + 2 * stride};
+    int *digit_off = t->hist.as<int>() + 3 * stride;
+    const bool direct = num_tiles <= kSortDirectTiles;  // offsets from the counts
+    const bool fused = num_tiles <= kSortFusedTiles;    // next histogram in the scatter
+    if (fused) NB_CUDA_TRY(cudaMemsetAsync(cnt[1], 0, sizeof(int) * 256 * (size_t)num_tiles, st));
+    int p = 0;
+    for (int shift = first_shift; shift < 64; shift += 8, ++p) {
+        const bool last = shift + 8 >= 64;
+        int *cur = fused ? cnt[p % 3] : cnt[0];
+        if (!fused || p == 0) {
+            radix_hist_kernel<<<num_tiles, 256, 0, st>>>(kin, n, shift, cur, num_tiles);
+            NB_LAUNCH_CHECK();
+        }
+        if (!direct) NB_TRY(scan_exclusive<int>(cur, 256 * num_tiles, digit_off, t->scan_tmp, st));
+        const bool next = fused && !last;
+        radix_scatter_kernel<<<num_tiles, 256, 0, st>>>(
+            kin, vin, kout, vout, n, shift, direct ? nullptr : digit_off, cur,
+            next ? cnt[(p + 1) % 3] : nullptr, next ? cnt[(p + 2) % 3] : nullptr, num_tiles);
         NB_LAUNCH_CHECK();
         std::swap(kin, kout);
         std::swap(vin, vout);
