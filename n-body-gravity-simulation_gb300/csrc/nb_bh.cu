@@ -389,13 +389,17 @@ scan_reduce_kernel(const T *__restrict__ in, int n, T *__restrict__ sums)
     if (threadIdx.x == 0) sums[blockIdx.x] = sh[0];
 }
 
-// Exclusive scan of the tile sums in place, one block of 1024 threads.
+// Exclusive scan of the tile sums in place, one block of up to 1024 threads
+// (a warp per 32 sums: the FP64 steps of a block scan run on one SM's narrow
+// FP64 pipe, so idle warps would only cost time).
 template <class T>
 __global__ void __launch_bounds__(1024) scan_top_kernel(T *__restrict__ a, int len)
 {
     __shared__ T warp_sums[33];
     const int t = threadIdx.x;
-    const int chunk = (len + 1023) / 1024;
+    if (t < 33) warp_sums[t] = Add<T>::zero();  // the warps the block lacks add nothing
+    __syncthreads();
+    const int chunk = (len + (int)blockDim.x - 1) / (int)blockDim.x;
     const int b = t * chunk, e = min(len, b + chunk);
     T s = Add<T>::zero();
     for (int k = b; k < e; ++k) s = Add<T>::op(s, a[k]);
@@ -1431,7 +1435,7 @@ nb_status scan_exclusive(const T *in, int n, T *out, DevBuf &tmp, cudaStream_t s
     T *sums = tmp.as<T>();
     scan_reduce_kernel<T><<<nb, 256, 0, st>>>(in, n, sums);
     NB_LAUNCH_CHECK();
-    scan_top_kernel<T><<<1, 1024, 0, st>>>(sums, nb);
+    scan_top_kernel<T><<<1, std::min(1024, 32 * div_up(nb, 32)), 0, st>>>(sums, nb);
     NB_LAUNCH_CHECK();
     scan_apply_kernel<T><<<nb, 256, 0, st>>>(in, n, sums, out);
     NB_LAUNCH_CHECK();
