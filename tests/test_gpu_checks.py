@@ -3,8 +3,9 @@ kernel family runs with its index checks on, no check fails, and the results
 are the same bits as the normal library's (the checks skip only accesses that
 would be out of range, and none is).  Each library runs in a child process
 (NBODY_GB300_LIB), since one process loads one build of the engine, with the
-autotuners off (NB_AUTOTUNE=0): timed tile shapes and j-splits could differ
-between two processes and change the summation order of the direct sums."""
+autotuners off (NB_AUTOTUNE=0): the mixed direct sums' bits do not depend on the
+tuned CTA shape, but the all-pairs ensemble kernel's timed i-bodies per lane
+would differ between two processes and change its summation order."""
 import os
 import subprocess
 import sys
