@@ -734,6 +734,13 @@ def run_ours(a, rank, world, local_rank):
     roofline["peak_fp32_tops"] = peak * 12.0 / 1e3
     roofline["traffic"] = profiled_traffic("direct_sorted_n65536.md") if n == N_BODIES else None
     roofline["algorithmic_bytes"] = 32 * n  # hi + lo mirror of every body, read once
+    # the same kernel against a measured FP32-pipe rate (packed FMAs on every
+    # SM, register-only probe), beside the lanes x clock peak above
+    fma_rate = nb.debug_fp32_rate()
+    roofline["peak_measured_fp32"] = {
+        "value": fma_rate / 12.0 / 1e9, "unit": "Ginteractions/s",
+        "frac": achieved / (fma_rate / 12.0 / 1e9), "fma_lane_tops": fma_rate / 1e12,
+        "basis": "nb_debug_fp32_rate (independent packed FMAs, best of 3 launches) / 12"}
 
     extras = {}
     if not a.skip_extras and rank == 0:

@@ -509,6 +509,13 @@ nb_status nb_debug_fail_device_allocations(int after);
  * failed check since the last call (and clears them), else NB_OK. */
 nb_status nb_debug_device_checks(int *enabled);
 
+/* Measured FP32-pipe rate of the current device: a register-only kernel of
+ * independent packed (f32x2) FMAs on every SM, best of three timed launches;
+ * *lane_ops_per_s = FMA lane operations per second.  A measured denominator for
+ * the FP32 rooflines of the force kernels, beside the lanes x clock figure.
+ * Not a reference call: benchmark support. */
+nb_status nb_debug_fp32_rate(double *lane_ops_per_s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -132,7 +132,55 @@ finish_kernel(const double *__restrict__ part, int nparts, const double *__restr
     }
 }
 
+// FP32 pipe rate probe: every thread runs kFmaRounds rounds of kFmaChains
+// independent packed FMAs on register values (no memory traffic in the loop)
+// and stores one sum, so that nothing is optimised away.
+constexpr int kFmaChains = 8, kFmaRounds = 4096;
+__global__ void __launch_bounds__(256) fma_rate_kernel(float seed, float *__restrict__ out)
+{
+    float2 a[kFmaChains];
+    const float2 m = make_float2(0.9999999f, 0.9999998f), c = make_float2(1e-7f, 2e-7f);
+#pragma unroll
+    for (int k = 0; k < kFmaChains; ++k)
+        a[k] = make_float2(seed + (float)(threadIdx.x + k), seed - (float)k);
+    for (int r = 0; r < kFmaRounds; ++r)
+#pragma unroll
+        for (int k = 0; k < kFmaChains; ++k) a[k] = __ffma2_rn(a[k], m, c);
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < kFmaChains; ++k) sum += a[k].x + a[k].y;
+    out[blockIdx.x * 256 + threadIdx.x] = sum;
+}
+
 } // namespace
+
+nb_status fp32_rate(double *lane_ops_per_s)
+{
+    const int blocks = 8 * device_props().num_sms;
+    DevBuf out;
+    NB_TRY(out.reserve(sizeof(float) * 256 * (size_t)blocks));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    NB_CUDA_TRY(cudaEventCreate(&e0));
+    NB_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    nb_status st = NB_OK;
+    for (int r = 0; r < 4 && st == NB_OK; ++r) {  // the first launch warms up
+        cudaEventRecord(e0, 0);
+        fma_rate_kernel<<<blocks, 256>>>(1.0f + r, out.as<float>());
+        cudaEventRecord(e1, 0);
+        if (cudaEventSynchronize(e1) != cudaSuccess) st = fail(NB_ERR_CUDA, "fp32 rate probe");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0) best = std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    out.release();
+    NB_TRY(st);
+    const double ops = (double)blocks * 256.0 * kFmaRounds * kFmaChains * 2.0;
+    *lane_ops_per_s = ops / (best * 1e-3);
+    return NB_OK;
+}
 
 nb_status diagnostics(const double *x, const double *y, const double *z, const double *vx,
                       const double *vy, const double *vz, const double *m, int n, double G,

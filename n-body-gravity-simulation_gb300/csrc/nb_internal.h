@@ -194,6 +194,9 @@ nb_status integrate_step(int integ, int n, double dt, double *const f[10], StepB
                          bool &forces_valid, const ForceFn &force, cudaStream_t st);
 
 // ---------------------------------------------------------------- diagnostics
+// Packed-FMA lane operations per second of the current device (a register-only
+// probe kernel, best of three timed launches).
+nb_status fp32_rate(double *lane_ops_per_s);
 nb_status diagnostics(const double *x, const double *y, const double *z, const double *vx,
                       const double *vy, const double *vz, const double *m, int n, double G,
                       double eps2, DevBuf &scratch, cudaStream_t st, nb_diag *out);

@@ -655,6 +655,12 @@ nb_status nb_debug_device_checks(int *enabled)
     return NB_OK;
 }
 
+nb_status nb_debug_fp32_rate(double *lane_ops_per_s)
+{
+    if (!lane_ops_per_s) return fail(NB_ERR_INVALID_ARGUMENT, "lane_ops_per_s is NULL");
+    return nb::fp32_rate(lane_ops_per_s);
+}
+
 nb_status nb_debug_fail_device_allocations(int after)
 {
     g_fail_allocs_after.store(after < 0 ? -1 : after);

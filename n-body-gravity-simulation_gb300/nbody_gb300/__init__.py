@@ -52,6 +52,7 @@ EXPORTS = [
     "nb_server_config_default", "nb_server_create", "nb_server_destroy", "nb_server_submit",
     "nb_server_tick", "nb_server_result", "nb_server_release", "nb_server_get_stats",
     "nb_server_cancel", "nb_debug_fail_device_allocations", "nb_debug_device_checks",
+    "nb_debug_fp32_rate",
 ]
 _NON_STATUS = {"nb_status_string", "nb_last_error", "nb_version", "nb_kernel_launch_count"}
 
@@ -222,6 +223,7 @@ def lib():
     L.nb_server_cancel.argtypes = [vp, C.c_int64]
     L.nb_debug_fail_device_allocations.argtypes = [C.c_int]
     L.nb_debug_device_checks.argtypes = [C.POINTER(C.c_int)]
+    L.nb_debug_fp32_rate.argtypes = [dp]
     for name in EXPORTS:
         f = getattr(L, name)
         if name not in _NON_STATUS:
@@ -642,6 +644,14 @@ def debug_device_checks() -> bool:
     enabled = C.c_int()
     _check(lib().nb_debug_device_checks(C.byref(enabled)), "nb_debug_device_checks")
     return bool(enabled.value)
+
+
+def debug_fp32_rate() -> float:
+    """nb_debug_fp32_rate: measured packed-FMA lane operations per second of
+    the current device (register-only probe kernel)."""
+    v = C.c_double(0.0)
+    _check(lib().nb_debug_fp32_rate(C.byref(v)), "nb_debug_fp32_rate")
+    return v.value
 
 
 def debug_fail_device_allocations(after: int):

@@ -276,3 +276,11 @@ def test_config_switch_between_paths(nb, oracle):
         s.config = nb.Config(method=nb.DIRECT_MIXED, G=2.0, softening=0.3)
         s.compute_forces()
         check_mixed(oracle, s.accelerations(), ref, st, 2.0, 0.3)
+
+
+def test_fp32_rate_probe(nb):
+    """nb_debug_fp32_rate measures the FMA lane rate the bench's measured
+    roofline uses: on a GB300 (152 SMs x 128 lanes at up to 2.07 GHz, 40.3e12
+    lane operations per second) it must land within a plausible band."""
+    r = nb.debug_fp32_rate()
+    assert 15e12 < r < 45e12, r
