@@ -259,27 +259,40 @@ def test_coincident_bodies_unsplittable_root(nb, oracle):
 
 @pytest.mark.parametrize("flags", [0, "quad", "ref"])
 @pytest.mark.parametrize("eps", [1e-3, 0.0])
-def test_group_walk_equals_preorder_walk(nb, monkeypatch, flags, eps):
+@pytest.mark.parametrize("workload", ["diskbulge", "clustered"])
+def test_group_walk_equals_preorder_walk(nb, oracle, monkeypatch, flags, eps, workload):
     """The default walk over child groups (an explicit stack per warp) and the
     stackless preorder walk (NB_BH_WALK=preorder) find the same interactions:
     equal monopole and body counts, forces equal up to the FP32 rounding of
     their different summation orders (a few 2^-24 sqrt(terms): up to ~6700
-    terms per body under the reference's opening rule)."""
+    terms per body under the reference's opening rule).  The clustered case
+    (two clumps of 1e-6 size, coincident bodies) has chains down to the deepest
+    level, the walk's deepest stacks."""
     flags = {0: 0, "quad": nb.BH_QUADRUPOLE, "ref": nb.BH_REFERENCE_OPENING}[flags]
-    state = nb.disk_bulge(40000, seed=12)
+    if workload == "diskbulge":
+        state, leaf = nb.disk_bulge(40000, seed=12), 8
+    else:
+        state, leaf = make(nb, oracle, "clustered")
     out = {}
     for walk in ("group", "preorder"):
         monkeypatch.setenv("NB_BH_WALK", walk)
-        with bh_sim(nb, state, eps=eps, flags=flags) as s:
+        with bh_sim(nb, state, eps=eps, flags=flags, leaf=leaf) as s:
             s.compute_forces()
             info = s.bh_info()
             out[walk] = (s.accelerations(), info["interactions_m2p"], info["interactions_p2p"])
     monkeypatch.delenv("NB_BH_WALK")
     assert out["group"][1:] == out["preorder"][1:]
     a, b = out["group"][0], out["preorder"][0]
+    assert all(np.isfinite(v).all() for v in a)
     mag = np.sqrt(sum(v * v for v in b))
     diff = np.sqrt(sum((u - v) ** 2 for u, v in zip(a, b)))
-    assert (diff / mag).max() < 1e-4 and np.median(diff / mag) < 4e-6
+    ok = mag > 0
+    assert np.array_equal(mag > 0, np.sqrt(sum(v * v for v in a)) > 0)
+    # bodies whose force nearly cancels carry larger relative differences:
+    # bound them against the largest force (FP32 sums of up to a few thousand
+    # terms in a different order), the typical body relatively; the equal
+    # interaction counts above are the exact check
+    assert diff.max() < 1e-4 * mag.max() and np.median(diff[ok] / mag[ok]) < 4e-6
 
 
 def test_deterministic(nb, oracle):
