@@ -753,7 +753,7 @@ node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__rest
             const int *__restrict__ offsets, const D4 *__restrict__ P,
             BHNode *__restrict__ nodes, unsigned char *__restrict__ node_depth,
             const int *__restrict__ pstart, int *__restrict__ parent,
-            unsigned char *__restrict__ octant, unsigned *__restrict__ occ,
+            unsigned char *__restrict__ octant, unsigned char *__restrict__ kidflag,
             BHStats *__restrict__ stats, int node_cap)
 {
     const int i = blockIdx.x * 256 + threadIdx.x;
@@ -786,7 +786,7 @@ node_kernel(const uint64_t *__restrict__ c, int n, int cap, const BHRoot *__rest
             const int oct = (int)((c[i] >> (63 - 3 * d)) & 7u);
             parent[id0 + k] = par;
             octant[id0 + k] = (unsigned char)oct;
-            if (NB_IN_RANGE(par, node_cap)) atomicOr(&occ[par], 1u << oct);
+            if (NB_IN_RANGE(par, node_cap)) kidflag[(size_t)par * 8 + oct] = 1;
         }
         leaves += leaf;
         maxd = max(maxd, d);
@@ -1176,8 +1176,9 @@ walk2_kernel(const BHNode *__restrict__ nodes, const int *__restrict__ total,
 // The group walk reads the children of a node together: gnodes holds, for
 // every internal node, its children's records contiguously and in Morton order
 // (a group), and group 0 is the root alone.  node_kernel records every node's
-// parent and octant and sets the octant's bit in the parent's mask;
-// alloc_groups_kernel claims a place for each group from a counter (every node
+// parent and octant and marks byte (parent, octant) of an 8-byte row per node
+// (each child its own byte: no atomics); alloc_groups_kernel packs a row into
+// the node's octant mask and claims a place for each group from a counter (every node
 // but the root is the child of exactly one node, so there are as many records
 // as nodes; where a group lands changes no result, since the walk's arithmetic
 // follows the groups' contents), and group_kernel writes each record with its
@@ -1192,18 +1193,29 @@ struct alignas(32) BHGNode {
 static_assert(sizeof(BHGNode) == 32, "group record layout");
 
 // A place for the group of every node with children (occ: the mask of its
-// non-empty octants): a block numbers its nodes' groups by a scan and claims
-// their span from the counter with one atomic.
+// non-empty octants, packed from its row of kidflag): a block numbers its
+// nodes' groups by a scan and claims their span from the counter with one
+// atomic.
 __global__ void __launch_bounds__(256)
-alloc_groups_kernel(const unsigned *__restrict__ occ, const int *__restrict__ total,
-                    int *__restrict__ base, int *__restrict__ next)
+alloc_groups_kernel(const unsigned char *__restrict__ kidflag, const int *__restrict__ total,
+                    unsigned *__restrict__ occ, int *__restrict__ base, int *__restrict__ next)
 {
     __shared__ int warp_sums[9];
     __shared__ int span0;
     const int num = *total;
     for (int k0 = blockIdx.x * 256; k0 < num; k0 += gridDim.x * 256) {
         const int k = k0 + threadIdx.x;
-        const int nk = k < num ? __popc(occ[k]) : 0;
+        unsigned o = 0;
+        if (k < num) {
+            const uint2 f = reinterpret_cast<const uint2 *>(kidflag)[k];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                o |= ((f.x >> (8 * b)) & 0xFFu) ? 1u << b : 0u;
+                o |= ((f.y >> (8 * b)) & 0xFFu) ? 1u << (b + 4) : 0u;
+            }
+            occ[k] = o;
+        }
+        const int nk = __popc(o);
         int span;
         const int off = block_exclusive<int, 8>(nk, warp_sums, &span);
         if (threadIdx.x == 0) span0 = atomicAdd(next, span);
@@ -1452,8 +1464,8 @@ struct BHTree {
     cudaEvent_t total_ready = nullptr;
     DevBuf part, root, keys0, keys1, vals0, vals1, hist, body, moments, prefix, chain_len,
         chain_depth, offsets, scan_tmp, nodes, node_depth, boxes, stats, moments2a, moments2b,
-        prefix2a, prefix2b, quad, pcen, pstart, parent, octant, occ, kbase, gnodes, gnk, gpcen,
-        gquad;
+        prefix2a, prefix2b, quad, pcen, pstart, parent, octant, occ, kidflag, kbase, gnodes, gnk,
+        gpcen, gquad;
     bool with_quad = false;     // the nodes carry quadrupoles (quad, 2 float4 per node)
     bool ref_open = false;      // the reference's opening rule (the child toward the body too)
     bool pcen_valid = false;    // pcen holds the parent centres of the current topology
@@ -1483,7 +1495,7 @@ void bh_destroy(BHTree *t)
                       &t->chain_depth, &t->offsets, &t->scan_tmp, &t->nodes, &t->node_depth,
                       &t->boxes, &t->stats, &t->moments2a, &t->moments2b, &t->prefix2a,
                       &t->prefix2b, &t->quad, &t->pcen, &t->pstart, &t->parent, &t->octant,
-                      &t->occ, &t->kbase, &t->gnodes,
+                      &t->occ, &t->kidflag, &t->kbase, &t->gnodes,
                       &t->gnk, &t->gpcen, &t->gquad};
     for (DevBuf *b : bufs) b->release();
     if (t->h_total) cudaFreeHost(t->h_total);
@@ -1776,8 +1788,8 @@ static nb_status group_nodes(BHTree *t, cudaStream_t st, bool recount)
         NB_TRY(t->kbase.reserve(sizeof(int) * ((size_t)slots + 1)));
         int *next = t->kbase.as<int>() + slots;  // the group counter (group 0: the root)
         NB_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(int), st));
-        alloc_groups_kernel<<<grid, 256, 0, st>>>(t->occ.as<unsigned>(), d_total(t),
-                                                  t->kbase.as<int>(), next);
+        alloc_groups_kernel<<<grid, 256, 0, st>>>(t->kidflag.as<unsigned char>(), d_total(t),
+                                                  t->occ.as<unsigned>(), t->kbase.as<int>(), next);
         NB_LAUNCH_CHECK();
     }
     NB_TRY(t->gnodes.reserve(sizeof(BHGNode) * (size_t)slots));
@@ -1880,6 +1892,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     NB_TRY(t->parent.reserve(sizeof(int) * cap));
     NB_TRY(t->octant.reserve(cap));
     NB_TRY(t->occ.reserve(sizeof(unsigned) * cap));
+    NB_TRY(t->kidflag.reserve(8 * cap));
     if (!t->h_total) NB_CUDA_TRY(cudaMallocHost(&t->h_total, sizeof(int)));
     if (!t->total_ready) NB_CUDA_TRY(cudaEventCreateWithFlags(&t->total_ready,
                                                               cudaEventDisableTiming));
@@ -1897,7 +1910,7 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
     t->num_nodes = -1;
     t->n = n;
     NB_CUDA_TRY(cudaMemsetAsync(stats, 0, offsetof(BHStats, total), st));
-    NB_CUDA_TRY(cudaMemsetAsync(t->occ.ptr, 0, sizeof(unsigned) * cap, st));
+    NB_CUDA_TRY(cudaMemsetAsync(t->kidflag.ptr, 0, 8 * cap, st));
     node_kernel<<<div_up(n, 256), 256, 0, st>>>(kin, n, leaf_capacity, root,
                                                 t->chain_len.as<int>(), t->chain_depth.as<int>(),
                                                 t->offsets.as<int>(), t->prefix.as<D4>(),
@@ -1905,7 +1918,8 @@ nb_status bh_compute(BHTree *t, const double *x, const double *y, const double *
                                                 t->node_depth.as<unsigned char>(),
                                                 t->pstart.as<int>(), t->parent.as<int>(),
                                                 t->octant.as<unsigned char>(),
-                                                t->occ.as<unsigned>(), stats, t->node_cap);
+                                                t->kidflag.as<unsigned char>(), stats,
+                                                t->node_cap);
     NB_LAUNCH_CHECK();
     if (quad) NB_TRY(compute_quads(t, x, y, z, m, n, st));
     t->pcen_valid = false;
