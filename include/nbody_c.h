@@ -513,6 +513,7 @@ nb_status nb_debug_device_checks(int *enabled);
  * independent packed (f32x2) FMAs on every SM, best of three timed launches;
  * *lane_ops_per_s = FMA lane operations per second.  A measured denominator for
  * the FP32 rooflines of the force kernels, beside the lanes x clock figure.
+ * Runs on the legacy default stream and waits for it (about 1 ms).
  * Not a reference call: benchmark support. */
 nb_status nb_debug_fp32_rate(double *lane_ops_per_s);
 

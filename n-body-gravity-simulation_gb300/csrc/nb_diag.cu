@@ -167,8 +167,10 @@ nb_status fp32_rate(double *lane_ops_per_s)
     for (int r = 0; r < 4 && st == NB_OK; ++r) {  // the first launch warms up
         cudaEventRecord(e0, 0);
         fma_rate_kernel<<<blocks, 256>>>(1.0f + r, out.as<float>());
+        const cudaError_t launched = cudaGetLastError();
         cudaEventRecord(e1, 0);
-        if (cudaEventSynchronize(e1) != cudaSuccess) st = fail(NB_ERR_CUDA, "fp32 rate probe");
+        if (launched != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+            st = fail(NB_ERR_CUDA, "fp32 rate probe");
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
         if (r > 0) best = std::min(best, ms);
