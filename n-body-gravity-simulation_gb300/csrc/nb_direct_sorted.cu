@@ -362,8 +362,10 @@ direct_sorted_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ l
 // terms into their double-single sums in increasing j; the warps' sums are
 // then added in warp order.  The result does not depend on timing.
 // ex[c n + i] = the FP64 value of body i's sum (sorted order), 0 if none.
+// At most 64 registers (four CTAs per SM): beside direct_sorted_kernel, whose
+// one-warp CTAs fill the register file, a leaner CTA displaces fewer of them.
 template <int IPT>
-__global__ void __launch_bounds__(kExactWarps * 32)
+__global__ void __launch_bounds__(kExactWarps * 32, 4)
 exact_pairs_kernel(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                    const float4 *__restrict__ box, int n, int nchunks, float eps2, float far2,
                    double eps2d, const double *__restrict__ root, float cap_per_n,
